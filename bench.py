@@ -1,0 +1,405 @@
+"""Benchmark of the int32 Floyd-Warshall APSP engine on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (default): the reference's maximum size, n = 32768 (a 4 GiB int32
+matrix), density 0.5, integer weights uniform in [1, 100], missing edge = INF,
+diagonal 0, seed 7, solved with the multi-layer (kappa = 4) schedule. Inputs
+are synthetic (the reference's generator with the weight range as a
+parameter). Metric: relaxations per second, n^3 per solve / solve time.
+
+One step = restore the pristine input (device-to-device copy) + one full
+solve. `value` is timed on the device with CUDA events over exactly K steps
+(inputs resident in HBM, 4 GiB > L2 so nothing stays cached between steps);
+`e2e` is the same metric through the C ABI with host buffers: every step
+copies the input from pinned host memory, solves, and copies the distance
+matrix back. With --gpus N (torchrun) every rank solves its own copy of the
+workload (replicas; the path has no data-parallel exchange) and `value` is
+the sum over ranks, timed by the slowest rank.
+
+--impl reference times the reference's CPU implementation of the path
+(baseline_cpu, src/fw_baseline_cpu.cpp:3-16, as restated by the oracle) on
+all host cores over bounded samples of the same workload, and additionally
+the reference's own GPU kernels (multi_layer_tiling_gpu, kappa 4, built for
+sm_103a from its sources) on the full workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "APSP relaxations/s (n^3/t)"
+UNIT = "relax/s"
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+VARIANTS = {"baseline_gpu": 0, "tiling_gpu": 1, "multi_layer_tiling_gpu": 2}
+
+
+def parse() -> argparse.Namespace:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=32768)
+    ap.add_argument("--density", type=float, default=0.5)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--wmin", type=int, default=1)
+    ap.add_argument("--wmax", type=int, default=100)
+    ap.add_argument("--algorithm", default="multi_layer_tiling_gpu", choices=list(VARIANTS))
+    ap.add_argument("--kappa", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target length of the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args) -> None:
+    import torch
+
+    import fw_cuda_gb300 as F
+
+    rank, world, local = dist_setup(args)
+    n = args.n
+    variant = VARIANTS[args.algorithm]
+    F.lib()
+    stream = torch.cuda.current_stream()
+
+    t0 = time.time()
+    h_in = torch.empty((n, n), dtype=torch.int32).pin_memory()
+    F.generate_graph(n, args.density, args.seed, args.wmin, args.wmax, out=h_in.numpy())
+    gen_s = time.time() - t0
+    pristine = h_in.cuda()
+    work = torch.empty_like(pristine)
+    relax = float(n) ** 3
+
+    def step():
+        work.copy_(pristine, non_blocking=True)
+        F.apsp_i32(work, n, 32, args.kappa, variant, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    peak_dpx, peak_mixed = F.measure_relax_peak(stream)
+    torch.cuda.synchronize()
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        F.profile_begin()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        prof = F.profile_end()
+    barrier(world)
+    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed = max_over_ranks(elapsed, world)
+    value = world * args.steps * relax / elapsed
+
+    # End to end through the C ABI with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        h_out = torch.empty((n, n), dtype=torch.int32).pin_memory()
+
+        def e2e_step():
+            work.copy_(h_in, non_blocking=True)
+            F.apsp_i32(work, n, 32, args.kappa, variant, stream)
+            h_out.copy_(work, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t2 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t1.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        t2.record(stream)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(t1.elapsed_time(t2) / 1e3, world)
+        e2e = {"value": world * args.steps * relax / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n * n, "d2h_bytes_per_step": 4 * n * n,
+               "ms_per_step": 1e3 * e2e_s / args.steps}
+        # Cheap sanity check of the last result: the diagonal is 0 and no entry
+        # exceeds its input edge weight.
+        assert torch.all(torch.diagonal(work) == 0).item()
+
+    rem = prof.get("fw_remainder", {"launches": 0, "total_ms": 0.0, "relaxations": 0.0})
+    roofline = None
+    if rem["launches"]:
+        achieved = rem["relaxations"] / (rem["total_ms"] / 1e3)
+        # algorithmic bytes of one remainder launch: its tiles read + written once, plus
+        # the two 128-wide panels it streams (n' = n - 128 rows/columns outside the pivot block)
+        nr = n - 128
+        bytes_per_launch = 8.0 * nr * nr + 2.0 * 4 * 128 * nr
+        hbm_gbs = bytes_per_launch * rem["launches"] / (rem["total_ms"] / 1e3) / 1e9
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+        roofline = {
+            "kernel": "fw_remainder_kernel",
+            "bound": "int_issue",
+            "achieved": achieved,
+            "peak": peak_mixed,
+            "unit": UNIT,
+            "frac": achieved / peak_mixed,
+            "peak_source": "measured live: register-only relaxation kernels (fw_measure_relax_peak), best instruction mix",
+            "dpx_only_peak": peak_dpx,
+            "frac_of_dpx_only": achieved / peak_dpx,
+            "traffic": None,
+            "avg_launch_ms": rem["total_ms"] / rem["launches"],
+            "relax_per_launch": rem["relaxations"] / rem["launches"],
+            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
+        }
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(h_in.numpy(), threads=1, seconds=args.cpu_seconds)
+
+    launches = sum(v["launches"] for v in prof.values())
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"APSP n={n} density={args.density} weights U[{args.wmin},{args.wmax}] "
+                                   f"seed={args.seed} ({args.algorithm}, kappa={args.kappa})",
+                       "n": n, "density": args.density, "seed": args.seed, "algorithm": args.algorithm,
+                       "kappa": args.kappa, "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (4 GiB matrix), restored from a pristine copy every step",
+                       "generate_s": round(gen_s, 2)},
+            "gpu_launches": launches,
+            "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()},
+            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def cpu_sample(W: np.ndarray, threads: int, seconds: float) -> dict:
+    """The oracle's baseline_cpu sweep over the first pivots of the full matrix
+    until about `seconds` have passed; relaxations/s = pivots * n^2 / t."""
+    from oracle import oracle as O
+
+    n = W.shape[0]
+    D = W.copy()
+    done, t0 = 0, time.perf_counter()
+    chunk = 1
+    while True:
+        O.fw_i32_pivots(D, n, done, done + chunk, threads)
+        done += chunk
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= n:
+            break
+        per = el / done
+        chunk = max(1, min(n - done, int((seconds - el) / per / 2) or 1))
+    return {"value": done * float(n) ** 2 / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"baseline_cpu k-i-j sweep (oracle restatement of src/fw_baseline_cpu.cpp:3-16), "
+                      f"pivots 0..{done - 1} of the n={n} workload matrix, {done} * n^2 relaxations in {el:.2f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import fw_cuda_gb300 as F
+    from oracle import oracle as O
+
+    n = args.n
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    W = np.empty((n, n), dtype=np.int32)
+    O.lib().oracle_generate_graph(W, n, args.density, args.seed, args.wmin, args.wmax)
+    gen_s = time.time() - t0
+    D = W.copy()
+    # Size one step to a few seconds of all-core work on this host.
+    t0 = time.perf_counter()
+    O.fw_i32_pivots(D, n, 0, 2, threads)
+    per_pivot = (time.perf_counter() - t0) / 2
+    pivots = max(1, min(n, int(4.0 / max(per_pivot, 1e-6))))
+    k = 2
+    for _ in range(args.warmup):
+        kk = min(n, k + pivots)
+        O.fw_i32_pivots(D, n, k, kk, threads)
+        k = kk if kk < n else 0
+    times = []
+    for _ in range(args.steps):
+        kk = min(n, k + pivots)
+        t0 = time.perf_counter()
+        O.fw_i32_pivots(D, n, k, kk, threads)
+        times.append((time.perf_counter() - t0, kk - k))
+        k = kk if kk < n else 0
+    tot_t = sum(t for t, _ in times)
+    tot_p = sum(p for _, p in times)
+    value = tot_p * float(n) ** 2 / tot_t
+    ref_gpu = reference_gpu(args, W)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"APSP n={n} density={args.density} weights U[{args.wmin},{args.wmax}] "
+                               f"seed={args.seed}", "n": n, "generate_s": round(gen_s, 2),
+                   "step": f"{pivots} pivots of the baseline_cpu k-i-j sweep over the full matrix"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps x {pivots} pivots (of {n}) of the baseline_cpu sweep "
+                                   f"(oracle restatement of src/fw_baseline_cpu.cpp:3-16) over the full n={n} "
+                                   f"matrix, rows split over {threads} host threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": ref_gpu,
+    }
+    del F
+    print(json.dumps(line), flush=True)
+
+
+def reference_gpu(args, W: np.ndarray):
+    """The reference's multi_layer_tiling_gpu (kappa 4) kernels, built for
+    sm_103a from its sources, timed on the full workload (one warm-up solve at
+    n=1024 first)."""
+    try:
+        import torch
+
+        from oracle import oracle as O
+
+        if not torch.cuda.is_available() or not O.refgpu_available():
+            return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
+        n = W.shape[0]
+        warm = torch.from_numpy(np.ascontiguousarray(W[:1024, :1024])).cuda()
+        O.refgpu_run("multi_layer_tiling_gpu", warm.data_ptr(), 1024, args.kappa)
+        d = torch.from_numpy(W).cuda()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        O.refgpu_run("multi_layer_tiling_gpu", d.data_ptr(), n, args.kappa)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        return {"algorithm": "multi_layer_tiling_gpu", "kappa": args.kappa, "value": float(n) ** 3 / el,
+                "unit": UNIT, "seconds_per_solve": el,
+                "how": "reference kernels (src/fw_multi_layer_tiling_gpu.cu) compiled for sm_103a, replayed with "
+                       "the reference launch loop, one solve timed on the host around a device synchronisation"}
+    except Exception as e:  # report, never fail the CPU line
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def main() -> None:
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+"""fw_cuda_gb300 — Python view of libfw103.so, the GB300 Floyd-Warshall engine.
+
+The engine itself is CUDA + C++ behind the C ABI in include/fw103.h; this
+module only loads that library with ctypes and mirrors the reference's
+algorithm registry (src/cuda_utils.cu:7-23, include/algo_types.h:9) so that
+Python callers and tests see the same names and argument meaning:
+
+    fn = get_gpu_algorithm_func("multi_layer_tiling_gpu")
+    fn(d_D, n, tile_size, kappa)     # d_D: int32 CUDA tensor (or device address), in place
+
+There is no CPU fallback: if the library is missing, importing works but every
+call raises FwLibraryMissing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+INF = 1_000_000_000  # include/constants.h:3
+MAX_N = 32769  # include/constants.h:5
+MAX_EDGE_WEIGHT = 25_000  # include/constants.h:7
+
+FW_OK = 0
+FW_ERR_INVALID_ARGUMENT = 1
+FW_ERR_CUDA = 2
+FW_ERR_NO_MEMORY = 3
+FW_ERR_TIMEOUT = 4
+FW_ERR_NOT_BUILT = 5
+
+VARIANT_BASELINE = 0
+VARIANT_TILING = 1
+VARIANT_MULTI_LAYER = 2
+
+# Every symbol include/fw103.h declares (checked by the CPU tests).
+EXPORTED_SYMBOLS = (
+    "fw_apsp_i32",
+    "fw_workspace_bytes_i32",
+    "fw_apsp_i32_ws",
+    "fw_generate_graph_i32",
+    "fw_last_error_string",
+    "fw_version",
+    "fw_profile_begin",
+    "fw_profile_end",
+    "fw_measure_relax_peak",
+)
+
+
+class FwError(RuntimeError):
+    """A libfw103 call returned a nonzero status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"fw103 status {status}: {msg}")
+        self.status = status
+
+
+class FwLibraryMissing(FwError):
+    def __init__(self, path: str):
+        super().__init__(FW_ERR_NOT_BUILT, f"{path} not found; run fw_cuda_gb300.build.build()")
+
+
+class KernelStats(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int64), ("total_ms", ctypes.c_double),
+                ("relaxations", ctypes.c_double)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.library_path()
+
+
+def lib():
+    """The loaded libfw103.so (raises FwLibraryMissing if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise FwLibraryMissing(path)
+    L = ctypes.CDLL(path)
+    vp, i64, c_int = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    L.fw_apsp_i32.argtypes = [vp, i64, c_int, c_int, c_int, vp]
+    L.fw_apsp_i32.restype = c_int
+    L.fw_workspace_bytes_i32.argtypes = [i64, c_int, c_int, c_int]
+    L.fw_workspace_bytes_i32.restype = ctypes.c_size_t
+    L.fw_apsp_i32_ws.argtypes = [vp, i64, c_int, c_int, c_int, vp, ctypes.c_size_t, vp]
+    L.fw_apsp_i32_ws.restype = c_int
+    L.fw_generate_graph_i32.argtypes = [vp, i64, ctypes.c_double, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32]
+    L.fw_generate_graph_i32.restype = c_int
+    L.fw_last_error_string.argtypes = []
+    L.fw_last_error_string.restype = ctypes.c_char_p
+    L.fw_version.argtypes = []
+    L.fw_version.restype = ctypes.c_char_p
+    L.fw_profile_begin.argtypes = []
+    L.fw_profile_begin.restype = c_int
+    L.fw_profile_end.argtypes = [ctypes.POINTER(KernelStats), c_int, ctypes.POINTER(c_int)]
+    L.fw_profile_end.restype = c_int
+    L.fw_measure_relax_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), vp]
+    L.fw_measure_relax_peak.restype = c_int
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != FW_OK:
+        raise FwError(rc, lib().fw_last_error_string().decode())
+
+
+def _ptr(x) -> int:
+    """Device address of a torch CUDA tensor, or an int address as is."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device address of {type(x)!r}")
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def apsp_i32(d_D, n: int, tile: int = 0, kappa: int = 0, variant: int = VARIANT_MULTI_LAYER, stream=None) -> None:
+    """In-place APSP on the device (enqueued on `stream`; no synchronisation)."""
+    _check(lib().fw_apsp_i32(_ptr(d_D), n, tile, kappa, variant, _stream(stream)))
+
+
+def workspace_bytes_i32(n: int, tile: int = 0, kappa: int = 0, variant: int = VARIANT_MULTI_LAYER) -> int:
+    return int(lib().fw_workspace_bytes_i32(n, tile, kappa, variant))
+
+
+def apsp_i32_ws(d_D, n: int, workspace, workspace_bytes: int, tile: int = 0, kappa: int = 0,
+                variant: int = VARIANT_MULTI_LAYER, stream=None) -> None:
+    _check(lib().fw_apsp_i32_ws(_ptr(d_D), n, tile, kappa, variant, _ptr(workspace), workspace_bytes,
+                                _stream(stream)))
+
+
+def generate_graph(n: int, density: float, seed: int, wmin: int = 0, wmax: int = MAX_EDGE_WEIGHT,
+                   out: np.ndarray | None = None) -> np.ndarray:
+    """The reference's random digraph (src/graph_generator.cpp:7-46) with a weight range."""
+    if out is None:
+        out = np.empty((n, n), dtype=np.int32)
+    assert out.dtype == np.int32 and out.flags.c_contiguous and out.size == n * n
+    _check(lib().fw_generate_graph_i32(out.ctypes.data, n, float(density), seed, wmin, wmax))
+    return out
+
+
+def version() -> str:
+    return lib().fw_version().decode()
+
+
+def profile_begin() -> None:
+    _check(lib().fw_profile_begin())
+
+
+def profile_end() -> dict:
+    """{kernel name: {"launches", "total_ms", "relaxations"}} since profile_begin()."""
+    cap = 16
+    arr = (KernelStats * cap)()
+    cnt = ctypes.c_int(0)
+    _check(lib().fw_profile_end(arr, cap, ctypes.byref(cnt)))
+    out = {}
+    for i in range(min(cnt.value, cap)):
+        s = arr[i]
+        out[s.name.decode()] = {"launches": int(s.launches), "total_ms": float(s.total_ms),
+                                "relaxations": float(s.relaxations)}
+    return out
+
+
+def measure_relax_peak(stream=None) -> tuple[float, float]:
+    """(DPX-only, best mixed) relaxations/s of the register-only kernels."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    _check(lib().fw_measure_relax_peak(ctypes.byref(a), ctypes.byref(b), _stream(stream)))
+    return a.value, b.value
+
+
+# ----------------------------------------------------- reference-style registry
+def _synchronising(variant: int):
+    def algo(d_D, n: int, tileSize: int = 0, kappa: int = 0) -> None:
+        import torch
+
+        apsp_i32(d_D, n, tileSize, kappa, variant, None)
+        torch.cuda.synchronize()
+
+    return algo
+
+
+fw_baseline_gpu = _synchronising(VARIANT_BASELINE)
+fw_tiling_gpu = _synchronising(VARIANT_TILING)
+fw_multi_layer_tiling_gpu = _synchronising(VARIANT_MULTI_LAYER)
+
+# src/cuda_utils.cu:7-11
+GPU_ALGORITHMS = {
+    "baseline_gpu": fw_baseline_gpu,
+    "tiling_gpu": fw_tiling_gpu,
+    "multi_layer_tiling_gpu": fw_multi_layer_tiling_gpu,
+}
+
+
+def get_gpu_algorithm_func(name: str):
+    """src/cuda_utils.cu:13-19 (std::out_of_range there, KeyError here)."""
+    try:
+        return GPU_ALGORITHMS[name]
+    except KeyError:
+        raise KeyError("ERROR: Unsupported GPU algorithm: " + name) from None
+
+
+def is_gpu_algorithm(name: str) -> bool:
+    """src/cuda_utils.cu:21-23."""
+    return name in GPU_ALGORITHMS

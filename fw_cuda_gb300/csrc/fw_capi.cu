@@ -1,0 +1,250 @@
+// C ABI of libfw103.so (declared in include/fw103.h): argument checks, status
+// codes, the per-(device, stream) workspace cache, per-kernel timing and the
+// host-side graph generator.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <random>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "fw103.h"
+#include "fw_internal.h"
+
+namespace fw {
+namespace {
+
+thread_local std::string t_last_error;
+
+// ----------------------------------------------------------------- workspace
+struct WsEntry {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+std::mutex g_ws_mutex;
+std::map<std::pair<int, cudaStream_t>, WsEntry> g_ws;
+
+// ----------------------------------------------------------------- profiling
+struct ProfState {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t next = 0;
+    struct Rec {
+        int kc;
+        cudaEvent_t a, b;
+        double relax;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> open;  // one pending start event per class
+};
+std::mutex g_prof_mutex;
+ProfState g_prof;
+const char* const kClassNames[KC_COUNT] = {"fw_diag", "fw_panel", "fw_remainder", "fw_pivot_step",
+                                           "fw_batched", "fw_forward_f32", "fw_backward_f32"};
+
+cudaEvent_t prof_event() {
+    if (g_prof.next == g_prof.pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        g_prof.pool.push_back(e);
+    }
+    return g_prof.pool[g_prof.next++];
+}
+
+}  // namespace
+
+int set_error(int status, const std::string& msg) {
+    t_last_error = msg;
+    return status;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+    return set_error(FW_ERR_CUDA, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+void prof_begin(KernelClass kc, cudaStream_t s) {
+    if (!g_prof.on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    cudaEvent_t e = prof_event();
+    if (!e) return;
+    cudaEventRecord(e, s);
+    g_prof.open[kc] = e;
+}
+
+void prof_end(KernelClass kc, cudaStream_t s, double relaxations) {
+    if (!g_prof.on) return;
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    cudaEvent_t a = g_prof.open[kc];
+    cudaEvent_t b = prof_event();
+    if (!a || !b) return;
+    cudaEventRecord(b, s);
+    g_prof.recs.push_back({kc, a, b, relaxations});
+    g_prof.open[kc] = nullptr;
+}
+
+void* workspace_get(cudaStream_t s, size_t bytes) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        set_error(FW_ERR_CUDA, "cudaGetDevice failed");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_ws_mutex);
+    WsEntry& w = g_ws[{dev, s}];
+    if (w.bytes >= bytes && w.ptr) return w.ptr;
+    if (w.ptr) {
+        // The old buffer may still be in use by work queued on `s`.
+        cudaStreamSynchronize(s);
+        cudaFree(w.ptr);
+        w.ptr = nullptr;
+        w.bytes = 0;
+    }
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(FW_ERR_NO_MEMORY, "workspace allocation of " + std::to_string(bytes) +
+                                        " bytes failed: " + cudaGetErrorString(e));
+        return nullptr;
+    }
+    w.ptr = p;
+    w.bytes = bytes;
+    return p;
+}
+
+int normalise_kappa(int kappa) { return (kappa <= 0 || kappa > 16) ? 4 : kappa; }
+
+}  // namespace fw
+
+using namespace fw;
+
+namespace {
+
+int check_apsp_args(const int32_t* d_D, int64_t n, int variant) {
+    if (d_D == nullptr) return set_error(FW_ERR_INVALID_ARGUMENT, "d_D is NULL");
+    if (n < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "n must be >= 1, got " + std::to_string(n));
+    // 64-bit offsets throughout; the per-pivot sweep puts one row per grid.y.
+    const int64_t nmax = (variant == FW_VARIANT_BASELINE) ? 65535 : 262144;
+    if (n > nmax)
+        return set_error(FW_ERR_INVALID_ARGUMENT,
+                         "n = " + std::to_string(n) + " exceeds " + std::to_string(nmax) + " for this variant");
+    if (variant != FW_VARIANT_BASELINE && variant != FW_VARIANT_TILING && variant != FW_VARIANT_MULTI_LAYER)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "unknown variant " + std::to_string(variant));
+    if ((reinterpret_cast<uintptr_t>(d_D) & 15u) != 0)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "d_D must be 16-byte aligned (cudaMalloc memory is)");
+    return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fw_last_error_string(void) { return t_last_error.c_str(); }
+
+const char* fw_version(void) { return "fw103 0.1.0 (sm_103a)"; }
+
+size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
+    (void)tile;
+    (void)kappa;
+    if (n < 1) return 0;
+    if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
+    return blocked_workspace_bytes(n);
+}
+
+int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
+                   size_t workspace_bytes, fw_stream_t stream) {
+    if (int rc = check_apsp_args(d_D, n, variant)) return rc;
+    (void)tile;  // fixed geometry, as in the reference (src/fw_tiling_gpu.cu:254-257)
+    kappa = normalise_kappa(kappa);
+    (void)kappa;
+    const size_t need = fw_workspace_bytes_i32(n, tile, kappa, variant);
+    if (d_workspace == nullptr || workspace_bytes < need)
+        return set_error(FW_ERR_INVALID_ARGUMENT,
+                         "workspace of " + std::to_string(need) + " bytes required, got " +
+                             std::to_string(workspace_bytes));
+    if ((reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
+    return blocked_solve(d_D, n, d_workspace, s);
+}
+
+int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {
+    if (int rc = check_apsp_args(d_D, n, variant)) return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t need = fw_workspace_bytes_i32(n, tile, kappa, variant);
+    void* ws = workspace_get(s, need);
+    if (!ws) return FW_ERR_NO_MEMORY;
+    return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, ws, need, stream);
+}
+
+int fw_generate_graph_i32(int32_t* h_out, int64_t n, double density, uint32_t seed, int32_t wmin, int32_t wmax) {
+    if (h_out == nullptr) return set_error(FW_ERR_INVALID_ARGUMENT, "h_out is NULL");
+    if (n < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "n must be >= 1");
+    if (!(density >= 0.0 && density <= 1.0)) return set_error(FW_ERR_INVALID_ARGUMENT, "density must be in [0, 1]");
+    if (wmin > wmax) return set_error(FW_ERR_INVALID_ARGUMENT, "wmin > wmax");
+    std::mt19937 gen(seed != 0 ? seed : std::random_device{}());
+    std::uniform_int_distribution<int32_t> weight(wmin, wmax);
+    std::bernoulli_distribution edge(density);
+    const size_t nn = static_cast<size_t>(n);
+    for (size_t i = 0; i < nn; ++i) {
+        int32_t* row = h_out + i * nn;
+        for (size_t j = 0; j < nn; ++j) {
+            row[j] = (i == j) ? 0 : (edge(gen) ? weight(gen) : FW_INF);
+        }
+    }
+    return FW_OK;
+}
+
+int fw_profile_begin(void) {
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    g_prof.on = true;
+    g_prof.next = 0;
+    g_prof.recs.clear();
+    g_prof.open.assign(KC_COUNT, nullptr);
+    return FW_OK;
+}
+
+int fw_profile_end(fw_kernel_stats* out, int cap, int* count) {
+    std::lock_guard<std::mutex> lk(g_prof_mutex);
+    g_prof.on = false;
+    std::vector<fw_kernel_stats> agg(KC_COUNT);
+    for (int k = 0; k < KC_COUNT; ++k) {
+        std::memset(&agg[k], 0, sizeof(fw_kernel_stats));
+        std::snprintf(agg[k].name, sizeof(agg[k].name), "%s", kClassNames[k]);
+    }
+    int status = FW_OK;
+    for (const auto& r : g_prof.recs) {
+        if (cudaEventSynchronize(r.b) != cudaSuccess) {
+            status = cuda_error(cudaGetLastError(), "cudaEventSynchronize");
+            continue;
+        }
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) {
+            status = cuda_error(cudaGetLastError(), "cudaEventElapsedTime");
+            continue;
+        }
+        agg[r.kc].launches += 1;
+        agg[r.kc].total_ms += ms;
+        agg[r.kc].relaxations += r.relax;
+    }
+    g_prof.recs.clear();
+    g_prof.next = 0;
+    int m = 0;
+    for (int k = 0; k < KC_COUNT; ++k) {
+        if (agg[k].launches == 0) continue;
+        if (out && m < cap) out[m] = agg[k];
+        ++m;
+    }
+    if (count) *count = m;
+    return status;
+}
+
+int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream) {
+    return measure_relax_peak(dpx_only, mixed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Shared device-side building blocks of the fw103 kernels (sm_103a).
+//
+// The relaxation is the reference's D[i][j] = min(D[i][j], D[i][k] + D[k][j])
+// in plain int32 arithmetic (src/fw_baseline_cpu.cpp:9-12,
+// src/fw_tiling_gpu.cu:235-245). Padding outside the matrix is INF, as in the
+// reference's tile loads (src/fw_tiling_gpu.cu:30-33), so a padded pivot
+// never wins: INF + INF = 2e9 still fits in int32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fw103.h"
+
+namespace fw {
+
+constexpr int kInf = FW_INF;
+
+// Blocked sweep geometry. A pivot block is 128 vertices wide; the matrix is
+// processed in 128 x 128 tiles by 256-thread CTAs, each thread holding an
+// 8 x 8 register micro-tile; operands stream through shared memory in slabs
+// of 32 pivots.
+constexpr int kTile = 128;
+constexpr int kSlab = 32;
+constexpr int kThreads = 256;
+constexpr int kStages = 3;
+constexpr int kSlabInts = kSlab * kTile;                 // one operand slab
+constexpr int kStageInts = 2 * kSlabInts;                // A slab + B slab
+constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
+
+// Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
+// ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns
+// tx*4 + {0..3} and 64 + tx*4 + {0..3}. Each group of 4 is one 16-byte
+// vector in shared memory and in global memory.
+__device__ __forceinline__ int own_row(int ty, int r) { return (r < 4) ? ty * 4 + r : 64 + ty * 4 + (r - 4); }
+__device__ __forceinline__ int own_col(int tx, int c) { return (c < 4) ? tx * 4 + c : 64 + tx * 4 + (c - 4); }
+
+// Two pivots folded into one accumulator. Form A issues two DPX add-min
+// instructions; form B issues two integer adds and one three-way DPX min.
+// The forms use different issue resources, so mixing them raises the
+// relaxation rate above what either reaches alone. Both compute
+// min(acc, a0 + b0, a1 + b1) exactly.
+// `form_a` is a compile-time constant at every call site once the micro-tile
+// loops are unrolled.
+__device__ __forceinline__ int relax2(bool form_a, int acc, int a0, int b0, int a1, int b1) {
+    if (form_a) {
+        return __viaddmin_s32(a1, b1, __viaddmin_s32(a0, b0, acc));
+    } else {
+        return __vimin3_s32(acc, a0 + b0, a1 + b1);
+    }
+}
+
+// One pivot pair of the 8 x 8 micro-tile update. `MIXA` of the 8 columns use
+// form A, the rest form B.
+template <int MIXA>
+__device__ __forceinline__ void relax_tile_pair(int (&acc)[8][8], const int (&a0)[8], const int (&b0)[8],
+                                                const int (&a1)[8], const int (&b1)[8]) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            acc[r][c] = relax2(c < MIXA, acc[r][c], a0[r], b0[c], a1[r], b1[c]);
+        }
+    }
+}
+
+// Reads the thread's 8 A values (pivot row kk of a k-major A slab) and 8 B
+// values into registers with four 16-byte shared loads.
+__device__ __forceinline__ void load_frag(const int* As, const int* Bs, int kk, int tx, int ty, int (&a)[8],
+                                          int (&b)[8]) {
+    const int4 a_lo = *reinterpret_cast<const int4*>(As + kk * kTile + ty * 4);
+    const int4 a_hi = *reinterpret_cast<const int4*>(As + kk * kTile + 64 + ty * 4);
+    const int4 b_lo = *reinterpret_cast<const int4*>(Bs + kk * kTile + tx * 4);
+    const int4 b_hi = *reinterpret_cast<const int4*>(Bs + kk * kTile + 64 + tx * 4);
+    a[0] = a_lo.x; a[1] = a_lo.y; a[2] = a_lo.z; a[3] = a_lo.w;
+    a[4] = a_hi.x; a[5] = a_hi.y; a[6] = a_hi.z; a[7] = a_hi.w;
+    b[0] = b_lo.x; b[1] = b_lo.y; b[2] = b_lo.z; b[3] = b_lo.w;
+    b[4] = b_hi.x; b[5] = b_hi.y; b[6] = b_hi.z; b[7] = b_hi.w;
+}
+
+// acc = min(acc, A (x) B) over one slab of kSlab pivots held in shared memory
+// (A k-major [kSlab][128], B k-major [kSlab][128]).
+template <int MIXA>
+__device__ __forceinline__ void relax_slab(int (&acc)[8][8], const int* As, const int* Bs, int tx, int ty) {
+#pragma unroll 1
+    for (int kk = 0; kk < kSlab; kk += 2) {
+        int a0[8], b0[8], a1[8], b1[8];
+        load_frag(As, Bs, kk, tx, ty, a0, b0);
+        load_frag(As, Bs, kk + 1, tx, ty, a1, b1);
+        relax_tile_pair<MIXA>(acc, a0, b0, a1, b1);
+    }
+}
+
+// ------------------------------------------------------------ async copies
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem_dst)), "l"(gmem_src)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+}  // namespace fw

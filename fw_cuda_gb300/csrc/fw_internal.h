@@ -1,0 +1,66 @@
+// Host-side internals shared by the fw103 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "fw103.h"
+
+namespace fw {
+
+// Records `msg` as this thread's last error and returns `status`.
+int set_error(int status, const std::string& msg);
+
+// Maps a CUDA error to FW_ERR_CUDA with a message naming `what`.
+int cuda_error(cudaError_t e, const char* what);
+
+#define FW_CUDA_TRY(call)                                              \
+    do {                                                               \
+        cudaError_t _e = (call);                                       \
+        if (_e != cudaSuccess) return ::fw::cuda_error(_e, #call);     \
+    } while (0)
+
+#define FW_LAUNCH_CHECK(what)                                          \
+    do {                                                               \
+        cudaError_t _e = cudaGetLastError();                           \
+        if (_e != cudaSuccess) return ::fw::cuda_error(_e, what);      \
+    } while (0)
+
+// Kernel classes timed by fw_profile_begin/fw_profile_end.
+enum KernelClass {
+    KC_DIAG = 0,
+    KC_PANEL,
+    KC_REMAINDER,
+    KC_PIVOT_STEP,
+    KC_BATCHED,
+    KC_FWD_F32,
+    KC_BWD_F32,
+    KC_COUNT
+};
+
+// Brackets one launch with events when profiling is on (no-ops otherwise).
+// `relaxations` is the algorithmic work the launch performs.
+void prof_begin(KernelClass kc, cudaStream_t s);
+void prof_end(KernelClass kc, cudaStream_t s, double relaxations);
+
+// Per-(device, stream) workspace owned by the library: at least `bytes`,
+// 256-byte aligned, kept for later calls. Returns nullptr (and sets the last
+// error) when allocation fails.
+void* workspace_get(cudaStream_t s, size_t bytes);
+
+// Normalised arguments of the blocked sweep.
+int normalise_kappa(int kappa);
+
+// Blocked-sweep launchers (fw_apsp_i32.cu).
+size_t blocked_workspace_bytes(int64_t n);
+int blocked_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
+size_t pivot_workspace_bytes(int64_t n);
+int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
+
+// Register-only relaxation-rate kernels (fw_peak.cu).
+int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);
+
+}  // namespace fw

@@ -1,0 +1,103 @@
+// Register-only relaxation-rate kernels: the integer issue ceiling that the
+// blocked sweep's roofline fraction is quoted against.
+//
+// Each thread keeps 16 accumulators and folds pivot pairs into them exactly
+// as the remainder kernel does (fw_common.cuh relax2), with operands taken
+// from other accumulators so that nothing can be hoisted out of the loop. No
+// memory is touched inside the timed loop.
+#include <cuda_runtime.h>
+
+#include "fw_common.cuh"
+#include "fw_internal.h"
+
+namespace fw {
+namespace {
+
+constexpr int kPeakIters = 4096;
+
+template <int MIXA>
+__global__ void __launch_bounds__(256) fw_peak_kernel(const int* __restrict__ in, int* __restrict__ out, int iters) {
+    int acc[4][4];
+    int a0[4], a1[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        a0[r] = in[(threadIdx.x + r) & 255];
+        a1[r] = in[256 + ((threadIdx.x + r) & 255)];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = in[512 + ((threadIdx.x + 4 * r + c) & 255)];
+    }
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                // Columns below MIXA/2 use form A (the 8-column tile maps to 4 here).
+                const int b0 = acc[(r + 1) & 3][c];
+                const int b1 = acc[r][(c + 1) & 3];
+                acc[r][c] = relax2(2 * c < MIXA, acc[r][c], a0[r], b0, a1[r], b1);
+            }
+        }
+    }
+    int s = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) s ^= acc[r][c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <int MIXA>
+int time_peak(int blocks, const int* in, int* out, cudaStream_t s, double* rate) {
+    cudaEvent_t e0, e1;
+    FW_CUDA_TRY(cudaEventCreate(&e0));
+    FW_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(e0, s);
+        fw_peak_kernel<MIXA><<<blocks, 256, 0, s>>>(in, out, kPeakIters);
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_error(e, "fw_peak_kernel");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;  // rep 0 warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // 16 accumulators x 2 relaxations per iteration.
+    *rate = (double)blocks * 256.0 * kPeakIters * 32.0 / (best * 1e-3);
+    return FW_OK;
+}
+
+}  // namespace
+
+int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8;
+    int *in = nullptr, *out = nullptr;
+    FW_CUDA_TRY(cudaMallocAsync(&in, 768 * sizeof(int), s));
+    FW_CUDA_TRY(cudaMallocAsync(&out, (size_t)blocks * 256 * sizeof(int), s));
+    FW_CUDA_TRY(cudaMemsetAsync(in, 0, 768 * sizeof(int), s));
+    double r8 = 0, r0 = 0, r3 = 0, r4 = 0;
+    int rc = time_peak<8>(blocks, in, out, s, &r8);
+    if (!rc) rc = time_peak<0>(blocks, in, out, s, &r0);
+    if (!rc) rc = time_peak<3>(blocks, in, out, s, &r3);
+    if (!rc) rc = time_peak<4>(blocks, in, out, s, &r4);
+    cudaFreeAsync(in, s);
+    cudaFreeAsync(out, s);
+    if (rc) return rc;
+    if (dpx_only) *dpx_only = r8;
+    double best = r0 > r3 ? r0 : r3;
+    best = best > r4 ? best : r4;
+    best = best > r8 ? best : r8;
+    if (mixed) *mixed = best;
+    return FW_OK;
+}
+
+}  // namespace fw

@@ -1,0 +1,117 @@
+/*
+ * fw103 — GB300 (sm_103a) Floyd-Warshall all-pairs shortest paths.
+ *
+ * C ABI of libfw103.so: plain pointers, sizes and status codes, callable from
+ * C, C++, ctypes or any other FFI. Device pointers are CUDA device addresses
+ * in the current device's context; `fw_stream_t` is a cudaStream_t (NULL =
+ * the legacy default stream). Every entry point except the host-only ones
+ * enqueues its work on the given stream and returns without synchronising;
+ * the C++ shims in fw103_algorithms.h add the reference's synchronising
+ * behaviour. On failure an entry point returns a nonzero fw_status and
+ * fw_last_error_string() describes it (per host thread).
+ *
+ * Semantics follow the reference project ddevedzic1/FW_CUDA: int32 weights,
+ * row-major n x n matrix, INF = 1e9 for a missing edge (include/constants.h:3),
+ * relaxation D[i][j] = min(D[i][j], D[i][k] + D[k][j]) in plain int32
+ * arithmetic (src/fw_baseline_cpu.cpp:9-12), 1 <= n <= 32769
+ * (include/constants.h:5).
+ */
+#ifndef FW103_H
+#define FW103_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FW_INF 1000000000       /* include/constants.h:3 */
+#define FW_MAX_N 32769          /* include/constants.h:5 */
+#define FW_MAX_EDGE_WEIGHT 25000 /* include/constants.h:7 */
+
+typedef struct CUstream_st* fw_stream_t;
+
+typedef enum fw_status {
+    FW_OK = 0,
+    FW_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, variant or layout */
+    FW_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
+    FW_ERR_NO_MEMORY = 3,        /* workspace allocation failed */
+    FW_ERR_TIMEOUT = 4,          /* a bounded device-side wait gave up */
+    FW_ERR_NOT_BUILT = 5         /* device code for this GPU is absent */
+} fw_status;
+
+/* Which of the reference's three GPU algorithms a call stands in for
+ * (src/cuda_utils.cu:7-11). Results are identical; the schedules differ. */
+typedef enum fw_variant {
+    FW_VARIANT_BASELINE = 0,    /* "baseline_gpu": one relaxation sweep per pivot */
+    FW_VARIANT_TILING = 1,      /* "tiling_gpu": blocked sweep, 128-wide pivot blocks */
+    FW_VARIANT_MULTI_LAYER = 2  /* "multi_layer_tiling_gpu": kappa pivot layers per pass */
+} fw_variant;
+
+/* ---------------------------------------------------------------- plain APSP */
+
+/* In-place APSP of the n x n int32 matrix at d_D.
+ * Replaces AlgorithmFuncGPU (include/algo_types.h:9) as implemented by
+ * fwBaselineGPU (src/fw_baseline_gpu.cu:16-32), fwTilingGPU
+ * (src/fw_tiling_gpu.cu:253-284) and fwMultiLayerTilingGPU
+ * (src/fw_multi_layer_tiling_gpu.cu:507-577). `tile` is accepted and ignored
+ * as in the reference; `kappa` is used by FW_VARIANT_MULTI_LAYER only, with
+ * the reference's normalisation (<= 0 or > 16 becomes 4,
+ * src/fw_multi_layer_tiling_gpu.cu:511-513). Uses a per-(device, stream)
+ * workspace that the library allocates on first use and keeps. */
+int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
+
+/* Bytes of device workspace fw_apsp_i32_ws needs for these arguments. */
+size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant);
+
+/* As fw_apsp_i32, with a caller-owned workspace of at least
+ * fw_workspace_bytes_i32() bytes (256-byte aligned); allocates nothing. */
+int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
+                   void* d_workspace, size_t workspace_bytes, fw_stream_t stream);
+
+/* ---------------------------------------------------------------- host side */
+
+/* The reference's random digraph (src/graph_generator.cpp:7-46) into a host
+ * buffer of n*n int32: std::mt19937(seed, or random_device when seed == 0),
+ * per ordered pair in row-major order: i == j -> 0; else a
+ * bernoulli(density) draw and, if it fires, a uniform integer in
+ * [wmin, wmax]; else FW_INF. wmin = 0, wmax = FW_MAX_EDGE_WEIGHT reproduces
+ * generateAlignedGraph1D byte for byte under the same libstdc++. */
+int fw_generate_graph_i32(int32_t* h_out, int64_t n, double density, uint32_t seed,
+                          int32_t wmin, int32_t wmax);
+
+/* Message of the last failure on this host thread ("" if none). */
+const char* fw_last_error_string(void);
+
+/* Library version string. */
+const char* fw_version(void);
+
+/* ---------------------------------------------------------------- measurement */
+
+/* Per-kernel timing over a window: fw_profile_begin() makes the library
+ * bracket each launch it issues with CUDA events on the launch stream;
+ * fw_profile_end() synchronises those events and reports, per kernel class,
+ * the launch count, summed device time and summed relaxations. */
+typedef struct fw_kernel_stats {
+    char name[32];
+    int64_t launches;
+    double total_ms;
+    double relaxations;
+} fw_kernel_stats;
+
+int fw_profile_begin(void);
+/* Writes up to `cap` entries; *count receives the number of kernel classes. */
+int fw_profile_end(fw_kernel_stats* out, int cap, int* count);
+
+/* Integer issue ceiling of this GPU for min-plus relaxations, measured with a
+ * register-only kernel (no memory traffic): relaxations per second when every
+ * relaxation is one DPX add-min instruction (dpx_only), and the best rate of
+ * the instruction mix the blocked kernels use (mixed). */
+int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FW103_H */

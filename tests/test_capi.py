@@ -1,0 +1,118 @@
+"""CPU-side checks of the C ABI: the library loads, exports every symbol the
+public header declares, and rejects bad arguments before touching a device
+(no compute call is made here)."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT, sha, load_json
+
+
+def declared_symbols() -> set[str]:
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        # C declarations at file scope: "<type> fw_name(" (not typedef / macros)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(fw_[a-z0-9_]+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declarations_are_exported(fw):
+    names = declared_symbols()
+    assert "fw_apsp_i32" in names and "fw_last_error_string" in names
+    L = fw.lib()
+    for name in sorted(names):
+        assert hasattr(L, name), f"{name} declared in include/ but not exported"
+    assert set(fw.EXPORTED_SYMBOLS) <= names
+
+
+def test_version(fw):
+    assert "sm_103a" in fw.version()
+
+
+def test_bad_arguments_fail_before_any_device_work(fw):
+    L = fw.lib()
+    # NULL matrix
+    assert L.fw_apsp_i32_ws(None, 16, 0, 0, 1, None, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"NULL" in L.fw_last_error_string()
+    fake = 0x7F0000000000  # never dereferenced: every check below fails first
+    assert L.fw_apsp_i32_ws(fake, 0, 0, 0, 1, None, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_apsp_i32_ws(fake, -5, 0, 0, 1, None, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_apsp_i32_ws(fake, 16, 0, 0, 7, None, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"variant" in L.fw_last_error_string()
+    assert L.fw_apsp_i32_ws(fake + 4, 16, 0, 0, 1, None, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"aligned" in L.fw_last_error_string()
+    # workspace missing / too small / misaligned
+    need = L.fw_workspace_bytes_i32(1000, 32, 4, 2)
+    assert need > 0
+    assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, None, need, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake, need - 1, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"workspace" in L.fw_last_error_string()
+    assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake + 16, need, None) == fw.FW_ERR_INVALID_ARGUMENT
+    # the per-pivot sweep puts one row per grid row
+    assert L.fw_apsp_i32_ws(fake, 70000, 0, 0, 0, fake, 1 << 40, None) == fw.FW_ERR_INVALID_ARGUMENT
+
+
+def test_workspace_sizes(fw):
+    # blocked: two 128-row panels with the leading dimension padded to 128
+    assert fw.workspace_bytes_i32(1, variant=1) == 2 * 128 * 128 * 4
+    assert fw.workspace_bytes_i32(32768, variant=2) == 2 * 128 * 32768 * 4
+    assert fw.workspace_bytes_i32(32769, variant=2) == 2 * 128 * (32768 + 128) * 4
+    # per-pivot: two row and two column snapshots
+    assert fw.workspace_bytes_i32(1001, variant=0) == 4 * 1004 * 4
+    assert fw.workspace_bytes_i32(0, variant=1) == 0
+
+
+def test_generator_matches_reference_hashes(fw, oracle):
+    for c in load_json("reference_cases.json")["cases"]:
+        if c["n"] > 1024:
+            continue
+        a = fw.generate_graph(c["n"], c["density"], c["seed"], c["wmin"], c["wmax"])
+        assert sha(a) == c["input_sha256"], c["id"]
+    a = fw.generate_graph(77, 0.4, 5, 1, 100)
+    assert np.array_equal(a, oracle.generate_graph(77, 0.4, 5, 1, 100))
+    assert a.min() == 0 and a[a < fw.INF].max() <= 100
+    assert np.all(np.diag(a) == 0)
+
+
+def test_generator_rejects_bad_arguments(fw):
+    L = fw.lib()
+    buf = np.empty(16, dtype=np.int32)
+    assert L.fw_generate_graph_i32(None, 4, 0.5, 1, 0, 10) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_generate_graph_i32(buf.ctypes.data, 4, 1.5, 1, 0, 10) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_generate_graph_i32(buf.ctypes.data, 4, 0.5, 1, 10, 0) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_generate_graph_i32(buf.ctypes.data, 0, 0.5, 1, 0, 10) == fw.FW_ERR_INVALID_ARGUMENT
+
+
+def test_registry_mirrors_reference(fw):
+    assert set(fw.GPU_ALGORITHMS) == {"baseline_gpu", "tiling_gpu", "multi_layer_tiling_gpu"}
+    assert fw.is_gpu_algorithm("tiling_gpu") and not fw.is_gpu_algorithm("baseline_cpu")
+    try:
+        fw.get_gpu_algorithm_func("nope")
+    except KeyError as e:
+        assert "Unsupported GPU algorithm: nope" in str(e)
+    else:
+        raise AssertionError("expected KeyError")
+
+
+def test_library_missing_fails_loudly(monkeypatch):
+    import fw_cuda_gb300 as F
+
+    monkeypatch.setattr(F, "_lib", None)
+    monkeypatch.setattr(F, "library_path", lambda: "/nonexistent/libfw103.so")
+    try:
+        F.lib()
+    except F.FwLibraryMissing as e:
+        assert "not found" in str(e)
+    else:
+        raise AssertionError("expected FwLibraryMissing")
+    assert ctypes is not None
