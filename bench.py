@@ -300,7 +300,7 @@ def cpu_sample(W: np.ndarray, threads: int, seconds: float) -> dict:
     done, t0 = 0, time.perf_counter()
     chunk = 1
     while True:
-        O.fw_i32_pivots(D, n, done, done + chunk, threads)
+        O.fw_i32_pivots(D, done, done + chunk, threads)
         done += chunk
         el = time.perf_counter() - t0
         if el >= seconds or done >= n:
@@ -328,19 +328,19 @@ def run_reference(args) -> None:
     D = W.copy()
     # Size one step to a few seconds of all-core work on this host.
     t0 = time.perf_counter()
-    O.fw_i32_pivots(D, n, 0, 2, threads)
+    O.fw_i32_pivots(D, 0, 2, threads)
     per_pivot = (time.perf_counter() - t0) / 2
     pivots = max(1, min(n, int(4.0 / max(per_pivot, 1e-6))))
     k = 2
     for _ in range(args.warmup):
         kk = min(n, k + pivots)
-        O.fw_i32_pivots(D, n, k, kk, threads)
+        O.fw_i32_pivots(D, k, kk, threads)
         k = kk if kk < n else 0
     times = []
     for _ in range(args.steps):
         kk = min(n, k + pivots)
         t0 = time.perf_counter()
-        O.fw_i32_pivots(D, n, k, kk, threads)
+        O.fw_i32_pivots(D, k, kk, threads)
         times.append((time.perf_counter() - t0, kk - k))
         k = kk if kk < n else 0
     tot_t = sum(t for t, _ in times)

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -19,7 +20,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 HOST = os.path.join(PKG, "host")
 LIBDIR = os.path.join(PKG, "_lib")
-OBJDIR = os.path.join(LIBDIR, "obj")
+# Objects are kept per host architecture so that a tree copied between an x86
+# and an Arm machine never links objects of the other one.
+OBJDIR = os.path.join(LIBDIR, "obj-" + platform.machine())
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -27,6 +30,9 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               f"-I{INCLUDE}", f"-I{CSRC}"]
 
 CUDA_SOURCES = ["fw_apsp_i32.cu", "fw_capi.cu", "fw_peak.cu"]
+HOST_LIB_SOURCES = ["algorithms.cpp"]  # compiled into libfw103.so
+TOOL_SOURCE = "runners.cpp"  # bench_runner / tests_runner (one binary, two names)
+TOOLS = ("bench_runner", "tests_runner")
 LIB_NAME = "libfw103.so"
 
 
@@ -60,6 +66,10 @@ def library_path() -> str:
     return os.path.join(LIBDIR, LIB_NAME)
 
 
+def tool_path(name: str) -> str:
+    return os.path.join(LIBDIR, name)
+
+
 def build(verbose: bool = False) -> str:
     """Compile every CUDA translation unit and link libfw103.so; returns its path."""
     os.makedirs(OBJDIR, exist_ok=True)
@@ -72,12 +82,30 @@ def build(verbose: bool = False) -> str:
         objs.append(o)
         if _stale(o, [s] + heads):
             jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+    for src in HOST_LIB_SOURCES:
+        s = os.path.join(HOST, src)
+        o = os.path.join(OBJDIR, src.replace(".cpp", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + heads):
+            jobs.append([nvcc(), *NVCC_FLAGS, "-c", s, "-o", o])
+    tool_obj = os.path.join(OBJDIR, TOOL_SOURCE.replace(".cpp", ".o"))
+    tsrc = os.path.join(HOST, TOOL_SOURCE)
+    if _stale(tool_obj, [tsrc] + heads):
+        jobs.append([nvcc(), *NVCC_FLAGS, "-c", tsrc, "-o", tool_obj])
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
     lib = library_path()
     if _stale(lib, objs):
         _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs])
+    tool = os.path.join(LIBDIR, TOOLS[0])
+    if _stale(tool, [tool_obj, lib]):
+        _run([nvcc(), *ARCH, "-o", tool, tool_obj, f"-L{LIBDIR}", "-lfw103", "-Xlinker", "-rpath,$ORIGIN"])
+    for alias in TOOLS[1:]:
+        ap = os.path.join(LIBDIR, alias)
+        if os.path.lexists(ap):
+            os.remove(ap)
+        os.symlink(TOOLS[0], ap)
     if verbose:
         print("built", lib)
     return lib
