@@ -181,14 +181,31 @@ def test_registry_functions_synchronise(fw, cuda, oracle):
 
 
 def test_reference_gpu_kernels_agree(fw, cuda, oracle):
-    """The reference's own kernels (built for sm_103a from its sources) on the same inputs."""
+    """The reference's own kernels (built for sm_103a from its sources) on the same inputs.
+
+    baseline_gpu, tiling_gpu and multi_layer_tiling_gpu with kappa = 1 must
+    agree with this engine bit for bit. For kappa >= 2 the reference's
+    multi-layer remainder kernel reuses its shared tiles for the next pivot
+    block without a barrier after the inner loop
+    (src/fw_multi_layer_tiling_gpu.cu:473-499), so its output varies from run
+    to run and can fall below the true distance on this GPU; there the
+    reference's baseline_cpu (the oracle of the reference's own test suite) is
+    the parity target, and the reference kernel's mismatch count is only
+    reported.
+    """
     if not oracle.refgpu_available():
         pytest.skip("reference kernels not built in this checkout")
     for n, d, s in ((128, 0.9, 42), (1000, 0.1, 5), (1024, 0.5, 6)):
         W = fw.generate_graph(n, d, s, 1, 100)
+        truth = oracle.fw_i32(W)
         mine = solve(fw, cuda, W, 2, kappa=4)
-        for name, kappa in (("tiling_gpu", 0), ("multi_layer_tiling_gpu", 2), ("multi_layer_tiling_gpu", 4),
-                            ("baseline_gpu", 0)):
+        assert np.array_equal(mine, truth)
+        for name, kappa in (("tiling_gpu", 0), ("multi_layer_tiling_gpu", 1), ("baseline_gpu", 0)):
             t = cuda.from_numpy(W).cuda()
             oracle.refgpu_run(name, t.data_ptr(), n, kappa)
             assert np.array_equal(t.cpu().numpy(), mine), (name, kappa, n)
+        for kappa in (2, 4):
+            t = cuda.from_numpy(W).cuda()
+            oracle.refgpu_run("multi_layer_tiling_gpu", t.data_ptr(), n, kappa)
+            bad = int(np.count_nonzero(t.cpu().numpy() != truth))
+            print(f"reference multi_layer_tiling_gpu kappa={kappa} n={n}: {bad} entries differ from baseline_cpu")
