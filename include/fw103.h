@@ -70,6 +70,18 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant);
 int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
                    void* d_workspace, size_t workspace_bytes, fw_stream_t stream);
 
+/* As fw_apsp_i32, for callers that cannot allocate device memory (a process
+ * whose pool already owns the GPU's free memory, code that must not take the
+ * implicit synchronisation of cudaMalloc/cudaFree, a plugin host without an
+ * allocator). No counterpart in the reference. The workspace is a fixed
+ * 8 MiB array inside the library's device image, held by every GPU that
+ * loads the library until exit; n > 8192 is rejected with
+ * FW_ERR_INVALID_ARGUMENT. All calls share that array: calls whose GPU work
+ * overlaps (other streams, other host threads) race and must be serialised
+ * by the caller. The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture. */
+int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
+
 /* ---------------------------------------------------------------- host side */
 
 /* The reference's random digraph (src/graph_generator.cpp:7-46) into a host
