@@ -64,6 +64,7 @@ def parse() -> argparse.Namespace:
                     help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-graphs measurement")
     return ap.parse_args()
 
 
@@ -270,6 +271,10 @@ def run_ours(args) -> None:
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
         }
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, F, torch, stream, world)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(h_in.numpy(), threads=1, seconds=args.cpu_seconds)
@@ -289,12 +294,58 @@ def run_ours(args) -> None:
             "gpu_launches": launches,
             "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()},
             "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary(),
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def run_batched(args, F, torch, stream, world) -> dict:
+    """4096 graphs, n log-uniform in [16, 512] (fw_cuda_gb300.workloads): one
+    autotuned, graph-captured batched launch per step, against looping the
+    single-graph entry point over the same graphs. Both time `steps` steps of
+    restore (device copy of the packed input) + solve with CUDA events."""
+    from fw_cuda_gb300 import workloads
+
+    sizes, offsets, packed = workloads.batched_graphs(F)
+    pristine = torch.from_numpy(packed).cuda()
+    work = torch.empty_like(pristine)
+    plan = F.BatchPlan(sizes, offsets)
+    schedule = plan.autotune(pristine, stream)
+    relax = plan.relaxations
+    base = work.data_ptr()
+
+    def timed(fn, steps):
+        for _ in range(max(1, args.warmup)):
+            work.copy_(pristine, non_blocking=True)
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            work.copy_(pristine, non_blocking=True)
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(a.elapsed_time(b) / 1e3, world) / steps
+
+    def loop():
+        for g in range(len(sizes)):
+            F.apsp_i32(base + 4 * int(offsets[g]), int(sizes[g]), 32, args.kappa, 2, stream)
+
+    t_batched = timed(lambda: plan.solve(work, stream), args.steps)
+    t_loop = timed(loop, max(1, min(args.steps, 2)))
+    plan.close()
+    count = len(sizes)
+    return {"workload": "4096 graphs, n log-uniform [16, 512], density U(0.05, 1), weights U[1, 100], seed 1234",
+            "graphs_per_s": world * count / t_batched, "relax_per_s": world * relax / t_batched,
+            "ms_per_step": 1e3 * t_batched, "schedule": schedule,
+            "loop_plain_graphs_per_s": world * count / t_loop, "loop_plain_ms_per_step": 1e3 * t_loop,
+            "speedup_vs_loop": t_loop / t_batched, "relaxations_per_step": relax}
 
 
 def cpu_sample(W: np.ndarray, threads: int, seconds: float) -> dict:

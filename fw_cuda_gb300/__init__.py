@@ -46,6 +46,12 @@ EXPORTED_SYMBOLS = (
     "fw_profile_begin",
     "fw_profile_end",
     "fw_measure_relax_peak",
+    "fw_batch_pack_offsets",
+    "fw_batch_plan_create",
+    "fw_batch_plan_autotune",
+    "fw_apsp_batched_i32",
+    "fw_batch_plan_describe",
+    "fw_batch_plan_destroy",
 )
 
 
@@ -102,6 +108,18 @@ def lib():
     L.fw_profile_end.restype = c_int
     L.fw_measure_relax_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak.restype = c_int
+    L.fw_batch_pack_offsets.argtypes = [vp, i64, vp, ctypes.POINTER(i64)]
+    L.fw_batch_pack_offsets.restype = c_int
+    L.fw_batch_plan_create.argtypes = [ctypes.POINTER(vp), vp, vp, i64]
+    L.fw_batch_plan_create.restype = c_int
+    L.fw_batch_plan_autotune.argtypes = [vp, vp, vp]
+    L.fw_batch_plan_autotune.restype = c_int
+    L.fw_apsp_batched_i32.argtypes = [vp, vp, vp]
+    L.fw_apsp_batched_i32.restype = c_int
+    L.fw_batch_plan_describe.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double)]
+    L.fw_batch_plan_describe.restype = c_int
+    L.fw_batch_plan_destroy.argtypes = [vp]
+    L.fw_batch_plan_destroy.restype = None
     _lib = L
     return L
 
@@ -184,6 +202,62 @@ def measure_relax_peak(stream=None) -> tuple[float, float]:
     a, b = ctypes.c_double(0), ctypes.c_double(0)
     _check(lib().fw_measure_relax_peak(ctypes.byref(a), ctypes.byref(b), _stream(stream)))
     return a.value, b.value
+
+
+# ----------------------------------------------------------------- batched APSP
+def pack_offsets(sizes) -> tuple[np.ndarray, int]:
+    """Element offsets of a dense packing (16-byte aligned starts) and its total size."""
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    offs = np.empty(len(sizes), dtype=np.int64)
+    total = ctypes.c_int64(0)
+    _check(lib().fw_batch_pack_offsets(sizes.ctypes.data, len(sizes), offs.ctypes.data, ctypes.byref(total)))
+    return offs, int(total.value)
+
+
+class BatchPlan:
+    """A planned batch of graphs (sizes + offsets into one packed int32 buffer)."""
+
+    def __init__(self, sizes, offsets=None):
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        if offsets is None:
+            offsets, self.total_elems = pack_offsets(self.sizes)
+        else:
+            offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+            self.total_elems = int(np.max(offsets + self.sizes.astype(np.int64) ** 2))
+        self.offsets = offsets
+        h = ctypes.c_void_p()
+        _check(lib().fw_batch_plan_create(ctypes.byref(h), self.sizes.ctypes.data, self.offsets.ctypes.data,
+                                          len(self.sizes)))
+        self._h = h
+
+    def autotune(self, d_packed, stream=None) -> str:
+        _check(lib().fw_batch_plan_autotune(self._h, _ptr(d_packed), _stream(stream)))
+        return self.describe()
+
+    def solve(self, d_packed, stream=None) -> None:
+        _check(lib().fw_apsp_batched_i32(self._h, _ptr(d_packed), _stream(stream)))
+
+    def describe(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        _check(lib().fw_batch_plan_describe(self._h, buf, 512, None))
+        return buf.value.decode()
+
+    @property
+    def relaxations(self) -> float:
+        r = ctypes.c_double(0)
+        _check(lib().fw_batch_plan_describe(self._h, None, 0, ctypes.byref(r)))
+        return r.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().fw_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ----------------------------------------------------- reference-style registry

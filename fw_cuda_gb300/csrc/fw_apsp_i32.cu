@@ -33,266 +33,81 @@
 
 #include "fw_common.cuh"
 #include "fw_internal.h"
+#include "fw_tile.cuh"
 
 namespace fw {
 namespace {
 
-// ------------------------------------------------------------------ loaders
-// Slab [k0, k0 + 32) x [c0, c0 + 128) of a k-major workspace buffer.
-__device__ __forceinline__ void load_kmajor_async(int* dst, const int* __restrict__ buf, int64_t ldp, int k0,
-                                                  int64_t c0, int tid) {
-#pragma unroll
-    for (int q = tid; q < kSlab * 32; q += kThreads) {
-        const int row = q >> 5, ch = q & 31;
-        cp_async16(dst + row * kTile + ch * 4, buf + (int64_t)(k0 + row) * ldp + c0 + ch * 4);
-    }
-}
-
-// Slab of D, rows [r0, r0 + 32), columns [c0, c0 + 128), INF outside the
-// matrix; row-major, which is k-major when the rows are pivots.
-template <bool VEC>
-__device__ __forceinline__ void load_d_rows(int* dst, const int* __restrict__ D, int64_t n, int64_t r0, int64_t c0,
-                                            int tid) {
-#pragma unroll
-    for (int q = tid; q < kSlab * 32; q += kThreads) {
-        const int row = q >> 5, ch = q & 31;
-        const int64_t gr = r0 + row, gc = c0 + ch * 4;
-        int* d = dst + row * kTile + ch * 4;
-        if (VEC) {
-            if (gr < n && gc < n) {
-                cp_async16(d, D + gr * n + gc);
-            } else {
-                *reinterpret_cast<int4*>(d) = make_int4(kInf, kInf, kInf, kInf);
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) d[e] = (gr < n && gc + e < n) ? D[gr * n + gc + e] : kInf;
-        }
-    }
-}
-
-// Transposed slab of D: dst[kk][i] = D[r0 + i][k0 + kk], INF outside.
-template <bool VEC>
-__device__ __forceinline__ void load_d_transposed(int* dst, const int* __restrict__ D, int64_t n, int64_t r0,
-                                                  int64_t k0, int tid) {
-#pragma unroll
-    for (int q = tid; q < kTile * 8; q += kThreads) {
-        const int i = q >> 3, ch = q & 7;
-        const int64_t gr = r0 + i, gc = k0 + ch * 4;
-        int v[4];
-        if (VEC && gr < n && gc < n) {
-            const int4 t = *reinterpret_cast<const int4*>(D + gr * n + gc);
-            v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) v[e] = (gr < n && gc + e < n) ? D[gr * n + gc + e] : kInf;
-        }
-#pragma unroll
-        for (int e = 0; e < 4; ++e) dst[(ch * 4 + e) * kTile + i] = v[e];
-    }
-}
-
-// The thread's 8 x 8 micro-tile of the 128 x 128 tile at (r0, c0) of D.
-template <bool VEC>
-__device__ __forceinline__ void load_acc(int (&acc)[8][8], const int* __restrict__ D, int64_t n, int64_t r0,
-                                         int64_t c0, int tx, int ty) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const int64_t gr = r0 + own_row(ty, r);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int64_t gc = c0 + h * 64 + tx * 4;
-            if (VEC) {
-                int4 t = make_int4(kInf, kInf, kInf, kInf);
-                if (gr < n && gc < n) t = *reinterpret_cast<const int4*>(D + gr * n + gc);
-                acc[r][h * 4 + 0] = t.x; acc[r][h * 4 + 1] = t.y;
-                acc[r][h * 4 + 2] = t.z; acc[r][h * 4 + 3] = t.w;
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    acc[r][h * 4 + e] = (gr < n && gc + e < n) ? D[gr * n + gc + e] : kInf;
-            }
-        }
-    }
-}
-
-template <bool VEC>
-__device__ __forceinline__ void store_acc(const int (&acc)[8][8], int* __restrict__ D, int64_t n, int64_t r0,
-                                          int64_t c0, int tx, int ty) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const int64_t gr = r0 + own_row(ty, r);
-        if (gr >= n) continue;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int64_t gc = c0 + h * 64 + tx * 4;
-            if (VEC) {
-                if (gc < n)
-                    *reinterpret_cast<int4*>(D + gr * n + gc) =
-                        make_int4(acc[r][h * 4 + 0], acc[r][h * 4 + 1], acc[r][h * 4 + 2], acc[r][h * 4 + 3]);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (gc + e < n) D[gr * n + gc + e] = acc[r][h * 4 + e];
-            }
-        }
-    }
-}
-
-// Row-major store of the micro-tile into a k-major workspace (no masking:
-// the workspace covers the padded extent).
-__device__ __forceinline__ void store_acc_ws(const int (&acc)[8][8], int* __restrict__ buf, int64_t ldp, int64_t c0,
-                                             int tx, int ty) {
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const int64_t row = own_row(ty, r);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            *reinterpret_cast<int4*>(buf + row * ldp + c0 + h * 64 + tx * 4) =
-                make_int4(acc[r][h * 4 + 0], acc[r][h * 4 + 1], acc[r][h * 4 + 2], acc[r][h * 4 + 3]);
-        }
-    }
-}
-
-// Transposed store: buf[c][r0 + r] = acc[r][c].
-__device__ __forceinline__ void store_acc_ws_transposed(const int (&acc)[8][8], int* __restrict__ buf, int64_t ldp,
-                                                        int64_t r0, int tx, int ty) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int64_t col = own_col(tx, c);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            *reinterpret_cast<int4*>(buf + col * ldp + r0 + h * 64 + ty * 4) =
-                make_int4(acc[h * 4 + 0][c], acc[h * 4 + 1][c], acc[h * 4 + 2][c], acc[h * 4 + 3][c]);
-        }
-    }
-}
-
-// Multi-stage cp.async pipeline over `nslab` operand slabs: acc = min(acc, A (x) B).
-// la(dst, s) / lb(dst, s) fill slab s of A / B (asynchronously or not).
-template <int MIXA, class LA, class LB>
-__device__ __forceinline__ void mainloop(int (&acc)[8][8], int nslab, int* smem, LA la, LB lb, int tx, int ty) {
-#pragma unroll
-    for (int s = 0; s < kStages - 1; ++s) {
-        if (s < nslab) {
-            la(smem + s * kStageInts, s);
-            lb(smem + s * kStageInts + kSlabInts, s);
-        }
-        cp_async_commit();
-    }
-    for (int kb = 0; kb < nslab; ++kb) {
-        cp_async_wait<kStages - 2>();
-        __syncthreads();
-        const int nxt = kb + kStages - 1;
-        if (nxt < nslab) {
-            int* st = smem + (nxt % kStages) * kStageInts;
-            la(st, nxt);
-            lb(st + kSlabInts, nxt);
-        }
-        cp_async_commit();
-        const int* st = smem + (kb % kStages) * kStageInts;
-        relax_slab<MIXA>(acc, st, st + kSlabInts, tx, ty);
-    }
-}
-
 // ------------------------------------------------------------------ kernels
 // Phase 1: closure of the pivot block D[P][P] by one CTA of 512 threads, each
-// holding a 4 x 8 register block (rows ty*4 + {0..3}, columns tx*8 + {0..7}).
-// Pivot k reads row k and column k from a shared-memory snapshot; the owners
-// of row k + 1 and column k + 1 publish them into the other buffer after
-// relaxing, so each pivot needs one barrier and no thread reads a value that
-// another thread writes in the same pivot step.
+// holding a 4 x 8 register block (BlockClosure<128, 32, 16>). Writes the
+// closed block back to D and into both workspace panels (transposed into
+// colT, as is into rowP).
 constexpr int kDiagThreads = 512;
+using DiagClosure = BlockClosure<kTile, 32, 16>;
 
 template <bool VEC>
 __global__ void __launch_bounds__(kDiagThreads, 1)
     fw_diag_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int64_t p0, int* __restrict__ colT,
                    int* __restrict__ rowP) {
-    __shared__ __align__(16) int prow[2][kTile];
-    __shared__ __align__(16) int pcol[2][kTile];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    int c[4][8];
+    __shared__ __align__(16) int prow[2 * kTile];
+    __shared__ __align__(16) int pcol[2 * kTile];
+    constexpr int RR = DiagClosure::RR, RC = DiagClosure::RC;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    int c[RR][RC];
     const int* src = D + p0 * n + p0;
     const int64_t rem = n - p0;  // valid rows / columns of the block
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int lr = ty * 4 + r;
+    for (int r = 0; r < RR; ++r) {
+        const int lr = ty * RR + r;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int lc = tx * 8 + h * 4;
+        for (int h = 0; h < RC; h += 4) {
+            const int lc = tx * RC + h;
             if (VEC) {
                 int4 t = make_int4(kInf, kInf, kInf, kInf);
                 if (lr < rem && lc < rem) t = *reinterpret_cast<const int4*>(src + lr * n + lc);
-                c[r][h * 4 + 0] = t.x; c[r][h * 4 + 1] = t.y; c[r][h * 4 + 2] = t.z; c[r][h * 4 + 3] = t.w;
+                c[r][h] = t.x; c[r][h + 1] = t.y; c[r][h + 2] = t.z; c[r][h + 3] = t.w;
             } else {
 #pragma unroll
-                for (int e = 0; e < 4; ++e) c[r][h * 4 + e] = (lr < rem && lc + e < rem) ? src[lr * n + lc + e] : kInf;
+                for (int e = 0; e < 4; ++e) c[r][h + e] = (lr < rem && lc + e < rem) ? src[lr * n + lc + e] : kInf;
             }
         }
     }
-    if (ty == 0) {
-        *reinterpret_cast<int4*>(&prow[0][tx * 8]) = make_int4(c[0][0], c[0][1], c[0][2], c[0][3]);
-        *reinterpret_cast<int4*>(&prow[0][tx * 8 + 4]) = make_int4(c[0][4], c[0][5], c[0][6], c[0][7]);
-    }
-    if (tx == 0) *reinterpret_cast<int4*>(&pcol[0][ty * 4]) = make_int4(c[0][0], c[1][0], c[2][0], c[3][0]);
-    __syncthreads();
-    for (int kb = 0; kb < kTile; kb += 8) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int buf = u & 1;  // (kb + u) & 1 with kb a multiple of 8
-            const int4 a = *reinterpret_cast<const int4*>(&pcol[buf][ty * 4]);
-            const int4 b0 = *reinterpret_cast<const int4*>(&prow[buf][tx * 8]);
-            const int4 b1 = *reinterpret_cast<const int4*>(&prow[buf][tx * 8 + 4]);
-            const int av[4] = {a.x, a.y, a.z, a.w};
-            const int bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int e = 0; e < 8; ++e) c[r][e] = __viaddmin_s32(av[r], bv[e], c[r][e]);
-            const int k1 = kb + u + 1;
-            if (k1 < kTile) {
-                const int sr = (u + 1) & 3, sc = (u + 1) & 7;
-                if (ty == (k1 >> 2)) {
-                    *reinterpret_cast<int4*>(&prow[buf ^ 1][tx * 8]) = make_int4(c[sr][0], c[sr][1], c[sr][2], c[sr][3]);
-                    *reinterpret_cast<int4*>(&prow[buf ^ 1][tx * 8 + 4]) =
-                        make_int4(c[sr][4], c[sr][5], c[sr][6], c[sr][7]);
-                }
-                if (tx == (k1 >> 3))
-                    *reinterpret_cast<int4*>(&pcol[buf ^ 1][ty * 4]) = make_int4(c[0][sc], c[1][sc], c[2][sc], c[3][sc]);
-            }
-            __syncthreads();
-        }
-    }
+    DiagClosure::run(c, prow, pcol, kTile, tx, ty, [] { __syncthreads(); });
     int* dst = D + p0 * n + p0;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int lr = ty * 4 + r;
+    for (int r = 0; r < RR; ++r) {
+        const int lr = ty * RR + r;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int lc = tx * 8 + h * 4;
-            const int4 v = make_int4(c[r][h * 4 + 0], c[r][h * 4 + 1], c[r][h * 4 + 2], c[r][h * 4 + 3]);
+        for (int h = 0; h < RC; h += 4) {
+            const int lc = tx * RC + h;
+            const int4 v = make_int4(c[r][h], c[r][h + 1], c[r][h + 2], c[r][h + 3]);
             if (VEC) {
                 if (lr < rem && lc < rem) *reinterpret_cast<int4*>(dst + lr * n + lc) = v;
             } else {
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                    if (lr < rem && lc + e < rem) dst[lr * n + lc + e] = c[r][h * 4 + e];
+                    if (lr < rem && lc + e < rem) dst[lr * n + lc + e] = c[r][h + e];
             }
             *reinterpret_cast<int4*>(rowP + (int64_t)lr * ldp + p0 + lc) = v;
         }
     }
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-        *reinterpret_cast<int4*>(colT + (int64_t)(tx * 8 + e) * ldp + p0 + ty * 4) =
-            make_int4(c[0][e], c[1][e], c[2][e], c[3][e]);
+    for (int e = 0; e < RC; ++e) {
+        int col[RR];
+#pragma unroll
+        for (int r = 0; r < RR; ++r) col[r] = c[r][e];
+        st_vec<RR>(colT + (int64_t)(tx * RC + e) * ldp + p0 + ty * RR, col);
+    }
 }
 
 // Phase 2: blockIdx.y == 0 -> row-panel tile D[P][J]; == 1 -> column-panel
 // tile D[I][P]; blockIdx.x enumerates the tiles other than the pivot tile.
-template <bool VEC, int MIXA>
+// `one` is the runtime 1 of the FMA-pipe additions (fw_common.cuh).
+template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_panel_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int pt, int nslab, int* __restrict__ colT,
-                    int* __restrict__ rowP) {
+                    int* __restrict__ rowP, int one) {
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int other = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
@@ -301,18 +116,18 @@ __global__ void __launch_bounds__(kThreads, 2)
     int acc[8][8];
     if (blockIdx.y == 0) {
         load_acc<VEC>(acc, D, n, p0, q0, tx, ty);
-        mainloop<MIXA>(
+        mainloop<kMixA>(
             acc, nslab, smem,
             [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, s * kSlab, p0, tid); },
-            [&](int* dst, int s) { load_d_rows<VEC>(dst, D, n, p0 + s * kSlab, q0, tid); }, tx, ty);
+            [&](int* dst, int s) { load_d_rows<VEC>(dst, D, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
         store_acc<VEC>(acc, D, n, p0, q0, tx, ty);
         store_acc_ws(acc, rowP, ldp, q0, tx, ty);
     } else {
         load_acc<VEC>(acc, D, n, q0, p0, tx, ty);
-        mainloop<MIXA>(
+        mainloop<kMixA>(
             acc, nslab, smem,
             [&](int* dst, int s) { load_d_transposed<VEC>(dst, D, n, q0, p0 + s * kSlab, tid); },
-            [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, p0, tid); }, tx, ty);
+            [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, p0, tid); }, tx, ty, one);
         store_acc<VEC>(acc, D, n, q0, p0, tx, ty);
         store_acc_ws_transposed(acc, colT, ldp, q0, tx, ty);
     }
@@ -320,10 +135,10 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 // Phase 3: tile (I, J), both different from the pivot tile:
 // D[I][J] = min(D[I][J], colT[:, I]^T (x) rowP[:, J]).
-template <bool VEC, int MIXA>
+template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int pt, int nslab,
-                        const int* __restrict__ colT, const int* __restrict__ rowP) {
+                        const int* __restrict__ colT, const int* __restrict__ rowP, int one) {
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
@@ -331,9 +146,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int64_t r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
     int acc[8][8];
     load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
-    mainloop<MIXA>(
+    mainloop<kMixA>(
         acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, s * kSlab, r0, tid); },
-        [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, c0, tid); }, tx, ty);
+        [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, c0, tid); }, tx, ty, one);
     store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
 }
 
@@ -386,29 +201,18 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-int g_mixa = -1;
-
-int mixa_setting() {
-    if (g_mixa < 0) {
-        const char* e = std::getenv("FW103_MIXA");
-        int v = e ? std::atoi(e) : 3;
-        g_mixa = (v == 0 || v == 3 || v == 8) ? v : 3;
-    }
-    return g_mixa;
-}
-
-template <bool VEC, int MIXA>
+template <bool VEC>
 int blocked_solve_impl(int32_t* D, int64_t n, int* colT, int* rowP, cudaStream_t s) {
     static bool attr_done = false;
     if (!attr_done) {
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC, MIXA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         kSmemBytes));
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_remainder_kernel<VEC, MIXA>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+        FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+        FW_CUDA_TRY(
+            cudaFuncSetAttribute(fw_remainder_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
         attr_done = true;
     }
     const int T = (int)((n + kTile - 1) / kTile);
     const int64_t ldp = (int64_t)T * kTile;
+    const int one = 1;
     for (int pt = 0; pt < T; ++pt) {
         const int64_t p0 = (int64_t)pt * kTile;
         const int64_t kv = n - p0 < kTile ? n - p0 : kTile;
@@ -419,12 +223,12 @@ int blocked_solve_impl(int32_t* D, int64_t n, int* colT, int* rowP, cudaStream_t
         prof_end(KC_DIAG, s, (double)kv * kv * kv);
         if (T > 1) {
             prof_begin(KC_PANEL, s);
-            fw_panel_kernel<VEC, MIXA><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP);
+            fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP, one);
             FW_LAUNCH_CHECK("fw_panel_kernel");
             prof_end(KC_PANEL, s, 2.0 * (double)(n - kv) * kv * kv);
             prof_begin(KC_REMAINDER, s);
-            fw_remainder_kernel<VEC, MIXA>
-                <<<dim3(T - 1, T - 1), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP);
+            fw_remainder_kernel<VEC>
+                <<<dim3(T - 1, T - 1), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP, one);
             FW_LAUNCH_CHECK("fw_remainder_kernel");
             prof_end(KC_REMAINDER, s, (double)(n - kv) * (n - kv) * kv);
         }
@@ -444,14 +248,7 @@ int blocked_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
     int* colT = static_cast<int*>(ws);
     int* rowP = colT + (size_t)kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    switch (mixa_setting()) {
-        case 0:
-            return vec ? blocked_solve_impl<true, 0>(D, n, colT, rowP, s) : blocked_solve_impl<false, 0>(D, n, colT, rowP, s);
-        case 8:
-            return vec ? blocked_solve_impl<true, 8>(D, n, colT, rowP, s) : blocked_solve_impl<false, 8>(D, n, colT, rowP, s);
-        default:
-            return vec ? blocked_solve_impl<true, 3>(D, n, colT, rowP, s) : blocked_solve_impl<false, 3>(D, n, colT, rowP, s);
-    }
+    return vec ? blocked_solve_impl<true>(D, n, colT, rowP, s) : blocked_solve_impl<false>(D, n, colT, rowP, s);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }

@@ -1,0 +1,539 @@
+// Batched APSP: thousands of independent graphs of uneven size in one
+// persistent launch. No reference counterpart; each graph's result is the
+// reference's k-i-j sweep (src/fw_baseline_cpu.cpp:6-15) of that graph.
+//
+// Layout: every graph g is an n_g x n_g int32 row-major matrix at element
+// offset offsets[g] of one packed device buffer, solved in place.
+//
+// Plan (host, once per batch shape): the graphs are sorted by size, largest
+// first, and split into buckets:
+//   bucket 0  n > 128        a whole CTA runs the blocked sweep on the graph
+//                            (128-wide pivot blocks, the same diag / panel /
+//                            remainder tiles and pipelined main loop as the
+//                            single-graph engine, the column panel kept in a
+//                            per-CTA workspace slice), tile after tile;
+//   bucket 1  64 < n <= 128  the graph lives in the registers of one CTA and
+//                            is closed by BlockClosure<128>;
+//   bucket 2  32 < n <= 64   likewise, padded to 64, by 1 or 4 graphs per CTA;
+//   bucket 3  16 < n <= 32   padded to 32, 1, 4 or 8 graphs per CTA;
+//   bucket 4        n <= 16  padded to 16, 1, 4 or 8 graphs per CTA.
+// The kernel is persistent: each CTA (or each group of threads inside it)
+// takes the next graph of the current bucket from an atomic counter, so
+// large graphs start first and small ones fill in behind them. The launch
+// (counter reset + kernel) is captured once into a CUDA graph per packed
+// buffer and replayed. The autotuner picks, per bucket, how many graphs share
+// a CTA, and the number of resident CTAs per SM, by timing the candidates on
+// a scratch copy of the batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "fw_common.cuh"
+#include "fw_internal.h"
+#include "fw_tile.cuh"
+
+namespace fw {
+namespace {
+
+constexpr int kBuckets = 5;
+constexpr int kBatchMaxN = 4096;
+
+struct BatchItem {
+    int64_t offset;
+    int32_t n;
+    int32_t index;
+};
+
+struct BatchSched {
+    int start[kBuckets];
+    int count[kBuckets];
+    int groups[kBuckets];  // graphs per CTA (small buckets): 1, 4 or 8
+};
+
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// ------------------------------------------------------------ small graphs
+// One graph of n <= NB held in the registers of a group of 256/G threads.
+// The graph (n*n contiguous ints) is staged through shared memory with
+// coalesced copies in and out; the pivot buffers of all groups come first.
+constexpr int kPivotInts = 8 * 4 * 32;  // >= G * 4 * NB for every (NB, G) used
+
+template <int NB, int G>
+__device__ __forceinline__ void small_bucket(int* __restrict__ packed, const BatchItem* __restrict__ items, int start,
+                                             int count, int* counter, int* smem, int* s_item) {
+    constexpr int GS = kThreads / G;
+    constexpr int TY = (GS == 256) ? 16 : 8;
+    constexpr int TX = GS / TY;
+    using Closure = BlockClosure<NB, TY, TX>;
+    constexpr int RR = Closure::RR, RC = Closure::RC;
+    static_assert(G * 4 * NB <= kPivotInts, "pivot buffers exceed their area");
+    static_assert(kPivotInts + G * NB * NB <= kSmemBytes / 4, "staging exceeds shared memory");
+    const int g = threadIdx.x / GS, gt = threadIdx.x % GS;
+    const int tx = gt % TX, ty = gt / TX;
+    int* prow = smem + g * 4 * NB;
+    int* pcol = prow + 2 * NB;
+    int* stage = smem + kPivotInts + g * NB * NB;
+    auto gsync = [g] {
+        if constexpr (GS == 256) {
+            __syncthreads();
+        } else if constexpr (GS == 32) {
+            __syncwarp();
+        } else {
+            named_sync(1 + g, GS);
+        }
+    };
+    for (;;) {
+        if (gt == 0) s_item[g] = atomicAdd(counter, 1);
+        gsync();
+        const int it = s_item[g];
+        gsync();
+        if (it >= count) break;
+        const BatchItem item = items[start + it];
+        int* Gm = packed + item.offset;
+        const int n = item.n;
+        const int nn = n * n;
+        for (int q = gt; q < nn; q += GS) stage[q] = Gm[q];
+        gsync();
+        int c[RR][RC];
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+            const int i = ty * RR + r;
+            const int* row = stage + i * n + tx * RC;
+#pragma unroll
+            for (int e = 0; e < RC; ++e) c[r][e] = (i < n && tx * RC + e < n) ? row[e] : kInf;
+        }
+        Closure::run(c, prow, pcol, n, tx, ty, gsync);
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+            const int i = ty * RR + r;
+            int* row = stage + i * n + tx * RC;
+#pragma unroll
+            for (int e = 0; e < RC; ++e)
+                if (i < n && tx * RC + e < n) row[e] = c[r][e];
+        }
+        gsync();
+        for (int q = gt; q < nn; q += GS) Gm[q] = stage[q];
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ void small_bucket_any(int groups, int* packed, const BatchItem* items, int start, int count,
+                                                 int* counter, int* smem, int* s_item) {
+    if constexpr (NB <= 32) {
+        if (groups == 8) return small_bucket<NB, 8>(packed, items, start, count, counter, smem, s_item);
+    }
+    if constexpr (NB <= 64) {
+        if (groups == 4) return small_bucket<NB, 4>(packed, items, start, count, counter, smem, s_item);
+    }
+    small_bucket<NB, 1>(packed, items, start, count, counter, smem, s_item);
+}
+
+// ------------------------------------------------------------ one large graph
+// The blocked sweep of one n x n graph by one CTA: per 128-wide pivot block,
+// the diagonal closure, the row and column panels, then the remainder tiles,
+// one tile at a time. colT (128 x ldw ints, this CTA's workspace slice) holds
+// the current column panel transposed.
+__device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int* __restrict__ colT, int64_t ldw,
+                                               int* smem, int one) {
+    using Closure = BlockClosure<kTile, 16, 16>;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int T = (n + kTile - 1) / kTile;
+    for (int pt = 0; pt < T; ++pt) {
+        const int p0 = pt * kTile;
+        const int kv = min(kTile, n - p0);
+        const int nslab = (kv + kSlab - 1) / kSlab;
+        {  // 1. diagonal block
+            int c[8][8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int i = ty * 8 + r;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int j = tx * 8 + e;
+                    c[r][e] = (i < kv && j < kv) ? Gm[(int64_t)(p0 + i) * n + p0 + j] : kInf;
+                }
+            }
+            Closure::run(c, smem, smem + 2 * kTile, kv, tx, ty, [] { __syncthreads(); });
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int i = ty * 8 + r;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int j = tx * 8 + e;
+                    if (i < kv && j < kv) Gm[(int64_t)(p0 + i) * n + p0 + j] = c[r][e];
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                int col[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) col[r] = c[r][e];
+                st_vec<8>(colT + (int64_t)(tx * 8 + e) * ldw + p0 + ty * 8, col);
+            }
+            __syncthreads();
+        }
+        int acc[8][8];
+        // 2. row panel: D[P][J] = min(D[P][J], Dg* (x) D[P][J])
+        for (int tj = 0; tj < T; ++tj) {
+            if (tj == pt) continue;
+            const int64_t q0 = (int64_t)tj * kTile;
+            load_acc<false>(acc, Gm, n, p0, q0, tx, ty);
+            mainloop<kMixA>(
+                acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, p0, tid); },
+                [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
+            store_acc<false>(acc, Gm, n, p0, q0, tx, ty);
+            __syncthreads();
+        }
+        // 3. column panel: D[I][P] = min(D[I][P], D[I][P] (x) Dg*), also into colT
+        for (int ti = 0; ti < T; ++ti) {
+            if (ti == pt) continue;
+            const int64_t r0 = (int64_t)ti * kTile;
+            load_acc<false>(acc, Gm, n, r0, p0, tx, ty);
+            mainloop<kMixA>(
+                acc, nslab, smem,
+                [&](int* dst, int s) { load_d_transposed<false>(dst, Gm, n, r0, p0 + s * kSlab, tid); },
+                [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, p0, tid); }, tx, ty, one);
+            store_acc<false>(acc, Gm, n, r0, p0, tx, ty);
+            store_acc_ws_transposed(acc, colT, ldw, r0, tx, ty);
+            __syncthreads();
+        }
+        // 4. remainder
+        for (int ti = 0; ti < T; ++ti) {
+            if (ti == pt) continue;
+            const int64_t r0 = (int64_t)ti * kTile;
+            for (int tj = 0; tj < T; ++tj) {
+                if (tj == pt) continue;
+                const int64_t q0 = (int64_t)tj * kTile;
+                load_acc<false>(acc, Gm, n, r0, q0, tx, ty);
+                mainloop<kMixA>(
+                    acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, r0, tid); },
+                    [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
+                store_acc<false>(acc, Gm, n, r0, q0, tx, ty);
+                __syncthreads();
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+    fw_batched_kernel(int* __restrict__ packed, const BatchItem* __restrict__ items, BatchSched sched,
+                      int* __restrict__ counters, int* __restrict__ ws, int64_t ldw, int one) {
+    extern __shared__ __align__(128) int smem[];
+    __shared__ int s_item[8];
+    // bucket 0: whole CTA per graph
+    int* colT = ws + (int64_t)blockIdx.x * kTile * ldw;
+    for (;;) {
+        if (threadIdx.x == 0) s_item[0] = atomicAdd(&counters[0], 1);
+        __syncthreads();
+        const int it = s_item[0];
+        __syncthreads();
+        if (it >= sched.count[0]) break;
+        const BatchItem item = items[sched.start[0] + it];
+        blocked_in_cta(packed + item.offset, item.n, colT, ldw, smem, one);
+    }
+    small_bucket<128, 1>(packed, items, sched.start[1], sched.count[1], &counters[1], smem, s_item);
+    __syncthreads();
+    small_bucket_any<64>(sched.groups[2], packed, items, sched.start[2], sched.count[2], &counters[2], smem, s_item);
+    __syncthreads();
+    small_bucket_any<32>(sched.groups[3], packed, items, sched.start[3], sched.count[3], &counters[3], smem, s_item);
+    __syncthreads();
+    small_bucket_any<16>(sched.groups[4], packed, items, sched.start[4], sched.count[4], &counters[4], smem, s_item);
+}
+
+int bucket_of(int n) {
+    if (n > 128) return 0;
+    if (n > 64) return 1;
+    if (n > 32) return 2;
+    if (n > 16) return 3;
+    return 4;
+}
+
+}  // namespace
+}  // namespace fw
+
+using namespace fw;
+
+struct fw_batch_plan {
+    int device = 0;
+    int64_t count = 0;
+    int32_t maxn = 0;
+    int64_t total_elems = 0;  // one past the last element any graph uses
+    double relaxations = 0;
+    BatchSched sched{};
+    int blocks_per_sm = 2;
+    int sms = 0;
+    int64_t ldw = 0;
+    BatchItem* d_items = nullptr;
+    int* d_counters = nullptr;
+    int* d_ws = nullptr;
+    int ws_ctas = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int32_t* exec_packed = nullptr;
+    std::string schedule;
+};
+
+namespace {
+
+void plan_describe(fw_batch_plan* p) {
+    char buf[256];
+    std::snprintf(buf, sizeof(buf),
+                  "graphs=%lld maxn=%d buckets[n>128:%d n<=128:%d n<=64:%d/g%d n<=32:%d/g%d n<=16:%d/g%d] "
+                  "ctas/sm=%d",
+                  (long long)p->count, p->maxn, p->sched.count[0], p->sched.count[1], p->sched.count[2],
+                  p->sched.groups[2], p->sched.count[3], p->sched.groups[3], p->sched.count[4], p->sched.groups[4],
+                  p->blocks_per_sm);
+    p->schedule = buf;
+}
+
+void drop_graph(fw_batch_plan* p) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+    p->exec_packed = nullptr;
+}
+
+int launch_direct(fw_batch_plan* p, int32_t* d_packed, cudaStream_t s) {
+    FW_CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, kBuckets * sizeof(int), s));
+    const int grid = p->sms * p->blocks_per_sm;
+    fw_batched_kernel<<<grid, kThreads, kSmemBytes, s>>>(d_packed, p->d_items, p->sched, p->d_counters, p->d_ws,
+                                                         p->ldw, 1);
+    FW_LAUNCH_CHECK("fw_batched_kernel");
+    return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fw_batch_pack_offsets(const int32_t* h_sizes, int64_t count, int64_t* h_offsets, int64_t* total_elems) {
+    if (!h_sizes || !h_offsets || count < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "bad arguments");
+    int64_t off = 0;
+    for (int64_t g = 0; g < count; ++g) {
+        if (h_sizes[g] < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "graph sizes must be >= 1");
+        h_offsets[g] = off;
+        off += ((int64_t)h_sizes[g] * h_sizes[g] + 3) & ~int64_t(3);  // 16-byte aligned starts
+    }
+    if (total_elems) *total_elems = off;
+    return FW_OK;
+}
+
+int fw_batch_plan_create(fw_batch_plan** out, const int32_t* h_sizes, const int64_t* h_offsets, int64_t count) {
+    if (!out || !h_sizes || !h_offsets || count < 1)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_batch_plan_create: NULL argument or count < 1");
+    if (count > (int64_t)1 << 30) return set_error(FW_ERR_INVALID_ARGUMENT, "too many graphs");
+    *out = nullptr;
+    std::vector<BatchItem> items(count);
+    int32_t maxn = 0;
+    int64_t end = 0;
+    double relax = 0;
+    for (int64_t g = 0; g < count; ++g) {
+        const int32_t n = h_sizes[g];
+        if (n < 1 || n > kBatchMaxN)
+            return set_error(FW_ERR_INVALID_ARGUMENT, "graph " + std::to_string(g) + ": n = " + std::to_string(n) +
+                                                          " outside [1, " + std::to_string(kBatchMaxN) + "]");
+        if (h_offsets[g] < 0) return set_error(FW_ERR_INVALID_ARGUMENT, "negative offset");
+        items[g] = {h_offsets[g], n, (int32_t)g};
+        maxn = std::max(maxn, n);
+        end = std::max(end, h_offsets[g] + (int64_t)n * n);
+        relax += (double)n * n * n;
+    }
+    // Graphs must not overlap (they are solved concurrently).
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return items[a].offset < items[b].offset; });
+    for (int64_t q = 1; q < count; ++q) {
+        const BatchItem& a = items[order[q - 1]];
+        if (a.offset + (int64_t)a.n * a.n > items[order[q]].offset)
+            return set_error(FW_ERR_INVALID_ARGUMENT, "graphs " + std::to_string(a.index) + " and " +
+                                                          std::to_string(items[order[q]].index) + " overlap");
+    }
+    std::stable_sort(items.begin(), items.end(), [](const BatchItem& a, const BatchItem& b) { return a.n > b.n; });
+    auto* p = new fw_batch_plan();
+    p->count = count;
+    p->maxn = maxn;
+    p->total_elems = end;
+    p->relaxations = relax;
+    for (int b = 0; b < kBuckets; ++b) {
+        p->sched.start[b] = 0;
+        p->sched.count[b] = 0;
+        p->sched.groups[b] = 1;
+    }
+    for (int64_t q = 0; q < count; ++q) {
+        const int b = bucket_of(items[q].n);
+        if (p->sched.count[b] == 0) p->sched.start[b] = (int)q;
+        p->sched.count[b]++;
+    }
+    // Defaults before tuning: pack small graphs 4 (n <= 64) or 8 (n <= 32) per CTA.
+    p->sched.groups[2] = 4;
+    p->sched.groups[3] = 8;
+    p->sched.groups[4] = 8;
+    int rc = FW_OK;
+    do {
+        if (cudaGetDevice(&p->device) != cudaSuccess) { rc = cuda_error(cudaGetLastError(), "cudaGetDevice"); break; }
+        if (cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+            rc = cuda_error(cudaGetLastError(), "cudaDeviceGetAttribute");
+            break;
+        }
+        p->ldw = ((int64_t)maxn + kTile - 1) / kTile * kTile;
+        p->ws_ctas = p->sms * 2;
+        if (cudaFuncSetAttribute(fw_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) !=
+            cudaSuccess) {
+            rc = cuda_error(cudaGetLastError(), "cudaFuncSetAttribute");
+            break;
+        }
+        if (cudaMalloc(&p->d_items, sizeof(BatchItem) * count) != cudaSuccess ||
+            cudaMalloc(&p->d_counters, sizeof(int) * kBuckets) != cudaSuccess ||
+            cudaMalloc(&p->d_ws, sizeof(int) * (size_t)kTile * p->ldw * p->ws_ctas) != cudaSuccess) {
+            cudaGetLastError();
+            rc = set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_create: device allocation failed");
+            break;
+        }
+        if (cudaMemcpy(p->d_items, items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = cuda_error(cudaGetLastError(), "cudaMemcpy(items)");
+            break;
+        }
+        if (cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            rc = cuda_error(cudaGetLastError(), "cudaStreamCreate");
+            break;
+        }
+    } while (false);
+    if (rc != FW_OK) {
+        fw_batch_plan_destroy(p);
+        return rc;
+    }
+    plan_describe(p);
+    *out = p;
+    return FW_OK;
+}
+
+void fw_batch_plan_destroy(fw_batch_plan* p) {
+    if (!p) return;
+    drop_graph(p);
+    if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+    cudaFree(p->d_items);
+    cudaFree(p->d_counters);
+    cudaFree(p->d_ws);
+    delete p;
+}
+
+int fw_batch_plan_describe(const fw_batch_plan* p, char* buf, size_t cap, double* relaxations) {
+    if (!p) return set_error(FW_ERR_INVALID_ARGUMENT, "NULL plan");
+    if (buf && cap) std::snprintf(buf, cap, "%s", p->schedule.c_str());
+    if (relaxations) *relaxations = p->relaxations;
+    return FW_OK;
+}
+
+int fw_apsp_batched_i32(fw_batch_plan* p, int32_t* d_packed, fw_stream_t stream) {
+    if (!p || !d_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_batched_i32: NULL plan or buffer");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (p->exec == nullptr || p->exec_packed != d_packed) {
+        drop_graph(p);
+        cudaGraph_t graph = nullptr;
+        FW_CUDA_TRY(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_direct(p, d_packed, p->cap_stream);
+        cudaError_t e = cudaStreamEndCapture(p->cap_stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&p->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            p->exec = nullptr;
+            return cuda_error(e, "cudaGraphInstantiate");
+        }
+        p->exec_packed = d_packed;
+    }
+    prof_begin(KC_BATCHED, s);
+    FW_CUDA_TRY(cudaGraphLaunch(p->exec, s));
+    prof_end(KC_BATCHED, s, p->relaxations);
+    return FW_OK;
+}
+
+// Times the candidate schedules on a scratch copy of the batch and keeps the
+// fastest: per small bucket the number of graphs per CTA, then the number of
+// resident CTAs per SM for the whole batch. Synchronises the stream.
+int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_t stream) {
+    if (!p || !d_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_batch_plan_autotune: NULL argument");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int32_t* scratch = nullptr;
+    const size_t bytes = sizeof(int32_t) * (size_t)p->total_elems;
+    if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_autotune: scratch copy allocation failed");
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const BatchSched full = p->sched;
+    auto time_once = [&](float* ms) -> int {
+        FW_CUDA_TRY(cudaMemcpyAsync(scratch, d_packed, bytes, cudaMemcpyDeviceToDevice, s));
+        FW_CUDA_TRY(cudaEventRecord(e0, s));
+        if (int rc = launch_direct(p, scratch, s)) return rc;
+        FW_CUDA_TRY(cudaEventRecord(e1, s));
+        FW_CUDA_TRY(cudaEventSynchronize(e1));
+        FW_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+        return FW_OK;
+    };
+    auto best_of = [&](float* out) -> int {  // one warm-up run, best of two timed runs
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            float ms = 0;
+            if (int rc = time_once(&ms)) return rc;
+            if (rep > 0) best = std::min(best, ms);
+        }
+        *out = best;
+        return FW_OK;
+    };
+    int rc = FW_OK;
+    const int options[kBuckets][3] = {{1, 1, 1}, {1, 1, 1}, {1, 4, 4}, {1, 4, 8}, {1, 4, 8}};
+    for (int b = 2; b < kBuckets && rc == FW_OK; ++b) {
+        if (full.count[b] == 0) continue;
+        // only bucket b runs
+        for (int q = 0; q < kBuckets; ++q) p->sched.count[q] = (q == b) ? full.count[q] : 0;
+        float best = 1e30f;
+        int choice = full.groups[b];
+        for (int o = 0; o < 3 && rc == FW_OK; ++o) {
+            if (o > 0 && options[b][o] == options[b][o - 1]) continue;
+            p->sched.groups[b] = options[b][o];
+            float ms = 0;
+            rc = best_of(&ms);
+            if (rc == FW_OK && ms < best) {
+                best = ms;
+                choice = options[b][o];
+            }
+        }
+        p->sched.groups[b] = choice;
+    }
+    for (int q = 0; q < kBuckets; ++q) p->sched.count[q] = full.count[q];
+    if (rc == FW_OK) {
+        float best = 1e30f;
+        int choice = p->blocks_per_sm;
+        for (int bps = 1; bps <= 2 && rc == FW_OK; ++bps) {
+            p->blocks_per_sm = bps;
+            float ms = 0;
+            rc = best_of(&ms);
+            if (rc == FW_OK && ms < best) {
+                best = ms;
+                choice = bps;
+            }
+        }
+        p->blocks_per_sm = choice;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(scratch);
+    drop_graph(p);  // the captured launch used the old schedule
+    plan_describe(p);
+    return rc;
+}
+
+}  // extern "C"

@@ -28,6 +28,11 @@ constexpr int kSlabInts = kSlab * kTile;                 // one operand slab
 constexpr int kStageInts = 2 * kSlabInts;                // A slab + B slab
 constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 
+// Number of the 8 micro-tile columns that fold a pivot pair with two DPX
+// add-min instructions; the other columns use form B (see relax2). 3 of 8
+// balances the ALU and FMA pipes best on GB300 (measured).
+constexpr int kMixA = 3;
+
 // Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
 // ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns
 // tx*4 + {0..3} and 64 + tx*4 + {0..3}. Each group of 4 is one 16-byte
@@ -35,31 +40,36 @@ constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 __device__ __forceinline__ int own_row(int ty, int r) { return (r < 4) ? ty * 4 + r : 64 + ty * 4 + (r - 4); }
 __device__ __forceinline__ int own_col(int tx, int c) { return (c < 4) ? tx * 4 + c : 64 + tx * 4 + (c - 4); }
 
-// Two pivots folded into one accumulator. Form A issues two DPX add-min
-// instructions; form B issues two integer adds and one three-way DPX min.
-// The forms use different issue resources, so mixing them raises the
-// relaxation rate above what either reaches alone. Both compute
-// min(acc, a0 + b0, a1 + b1) exactly.
-// `form_a` is a compile-time constant at every call site once the micro-tile
-// loops are unrolled.
-__device__ __forceinline__ int relax2(bool form_a, int acc, int a0, int b0, int a1, int b1) {
+// a * one + b with `one` a runtime 1: an integer multiply-add, which issues on
+// the FMA pipe, instead of an add, which would issue on the ALU pipe that the
+// DPX instructions already saturate. Exact: the low 32 bits of a*1 + b.
+__device__ __forceinline__ int add_on_fma(int a, int b, int one) {
+    int s;
+    asm("mad.lo.s32 %0, %1, %3, %2;" : "=r"(s) : "r"(a), "r"(b), "r"(one));
+    return s;
+}
+
+// Two pivots folded into one accumulator: min(acc, a0 + b0, a1 + b1).
+// Form A: two DPX add-min instructions (ALU pipe). Form B: two multiply-adds
+// (FMA pipe) and one three-way DPX min (ALU pipe). `form_a` is a compile-time
+// constant at every call site once the micro-tile loops are unrolled.
+__device__ __forceinline__ int relax2(bool form_a, int acc, int a0, int b0, int a1, int b1, int one) {
     if (form_a) {
         return __viaddmin_s32(a1, b1, __viaddmin_s32(a0, b0, acc));
     } else {
-        return __vimin3_s32(acc, a0 + b0, a1 + b1);
+        return __vimin3_s32(acc, add_on_fma(a0, b0, one), add_on_fma(a1, b1, one));
     }
 }
 
-// One pivot pair of the 8 x 8 micro-tile update. `MIXA` of the 8 columns use
-// form A, the rest form B.
+// One pivot pair of the 8 x 8 micro-tile update; columns below MIXA use form A.
 template <int MIXA>
 __device__ __forceinline__ void relax_tile_pair(int (&acc)[8][8], const int (&a0)[8], const int (&b0)[8],
-                                                const int (&a1)[8], const int (&b1)[8]) {
+                                                const int (&a1)[8], const int (&b1)[8], int one) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            acc[r][c] = relax2(c < MIXA, acc[r][c], a0[r], b0[c], a1[r], b1[c]);
+            acc[r][c] = relax2(c < MIXA, acc[r][c], a0[r], b0[c], a1[r], b1[c], one);
         }
     }
 }
@@ -81,13 +91,13 @@ __device__ __forceinline__ void load_frag(const int* As, const int* Bs, int kk, 
 // acc = min(acc, A (x) B) over one slab of kSlab pivots held in shared memory
 // (A k-major [kSlab][128], B k-major [kSlab][128]).
 template <int MIXA>
-__device__ __forceinline__ void relax_slab(int (&acc)[8][8], const int* As, const int* Bs, int tx, int ty) {
+__device__ __forceinline__ void relax_slab(int (&acc)[8][8], const int* As, const int* Bs, int tx, int ty, int one) {
 #pragma unroll 1
     for (int kk = 0; kk < kSlab; kk += 2) {
         int a0[8], b0[8], a1[8], b1[8];
         load_frag(As, Bs, kk, tx, ty, a0, b0);
         load_frag(As, Bs, kk + 1, tx, ty, a1, b1);
-        relax_tile_pair<MIXA>(acc, a0, b0, a1, b1);
+        relax_tile_pair<MIXA>(acc, a0, b0, a1, b1, one);
     }
 }
 
@@ -107,5 +117,94 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
+
+// ------------------------------------------------------------ small vectors
+template <int R>
+__device__ __forceinline__ void ld_vec(const int* p, int (&v)[R]) {
+    if constexpr (R % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < R; q += 4) {
+            const int4 t = *reinterpret_cast<const int4*>(p + q);
+            v[q] = t.x; v[q + 1] = t.y; v[q + 2] = t.z; v[q + 3] = t.w;
+        }
+    } else if constexpr (R == 2) {
+        const int2 t = *reinterpret_cast<const int2*>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < R; ++q) v[q] = p[q];
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void st_vec(int* p, const int (&v)[R]) {
+    if constexpr (R % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < R; q += 4) *reinterpret_cast<int4*>(p + q) = make_int4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+    } else if constexpr (R == 2) {
+        *reinterpret_cast<int2*>(p) = make_int2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < R; ++q) p[q] = v[q];
+    }
+}
+
+// ------------------------------------------------------------ block closure
+// Min-plus closure (the k-sequential Floyd-Warshall sweep) of an NB x NB block
+// held in registers by a TY x TX grid of threads, each owning rows
+// ty*RR .. ty*RR+RR-1 and columns tx*RC .. tx*RC+RC-1. Pivot k reads row k
+// and column k from a shared-memory snapshot; after relaxing, the owners of
+// row k+1 and column k+1 publish them into the other buffer, so each pivot
+// costs one barrier and no thread reads a value another thread writes in the
+// same pivot step. prow / pcol: 2 * NB ints each, 16-byte aligned. `kcount`
+// pivots are applied, rounded up to the unroll width (padded pivots are INF
+// rows and columns and change nothing). `sync` is the barrier of the
+// participating threads.
+template <int NB, int TY, int TX>
+struct BlockClosure {
+    static constexpr int RR = NB / TY;
+    static constexpr int RC = NB / TX;
+    static constexpr int U = RR > RC ? RR : RC;
+
+    template <class Sync>
+    __device__ __forceinline__ static void run(int (&c)[RR][RC], int* prow, int* pcol, int kcount, int tx, int ty,
+                                               Sync sync) {
+        if (ty == 0) st_vec<RC>(prow + tx * RC, c[0]);
+        if (tx == 0) {
+            int col[RR];
+#pragma unroll
+            for (int r = 0; r < RR; ++r) col[r] = c[r][0];
+            st_vec<RR>(pcol + ty * RR, col);
+        }
+        sync();
+        for (int kb = 0; kb < kcount; kb += U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int k = kb + u;
+                const int buf = k & 1;
+                int a[RR], b[RC];
+                ld_vec<RR>(pcol + buf * NB + ty * RR, a);
+                ld_vec<RC>(prow + buf * NB + tx * RC, b);
+#pragma unroll
+                for (int r = 0; r < RR; ++r)
+#pragma unroll
+                    for (int e = 0; e < RC; ++e) c[r][e] = __viaddmin_s32(a[r], b[e], c[r][e]);
+                const int k1 = k + 1;
+                if (k1 < NB) {
+                    // k1 % RR and k1 % RC, static because kb is a multiple of U
+                    const int sr = (u + 1) % RR, sc = (u + 1) % RC;
+                    if (ty == k1 / RR) st_vec<RC>(prow + (buf ^ 1) * NB + tx * RC, c[sr]);
+                    if (tx == k1 / RC) {
+                        int col[RR];
+#pragma unroll
+                        for (int r = 0; r < RR; ++r) col[r] = c[r][sc];
+                        st_vec<RR>(pcol + (buf ^ 1) * NB + ty * RR, col);
+                    }
+                }
+                sync();
+            }
+        }
+    }
+};
 
 }  // namespace fw

@@ -82,6 +82,36 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
  * address (cudaGetSymbolAddress); make it before any stream capture. */
 int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
 
+/* ---------------------------------------------------------------- batched APSP */
+
+/* Many independent graphs solved in one persistent launch. No counterpart in
+ * the reference; each graph's result is the reference's baseline_cpu sweep
+ * (src/fw_baseline_cpu.cpp:6-15) of that graph. Graph g is an n_g x n_g
+ * int32 row-major matrix at element offset offsets[g] of one packed device
+ * buffer (1 <= n_g <= 4096, graphs must not overlap), solved in place. */
+typedef struct fw_batch_plan fw_batch_plan;
+
+/* Offsets for a dense packing with 16-byte aligned graph starts; writes
+ * count offsets and the total element count of the packed buffer. */
+int fw_batch_pack_offsets(const int32_t* h_sizes, int64_t count, int64_t* h_offsets, int64_t* total_elems);
+
+/* Sorts the graphs into size buckets, uploads the work list and allocates
+ * the per-CTA workspace on the current device. */
+int fw_batch_plan_create(fw_batch_plan** plan, const int32_t* h_sizes, const int64_t* h_offsets, int64_t count);
+
+/* Chooses the per-bucket schedule (graphs per CTA, CTAs per SM) by timing the
+ * candidates on a scratch copy of d_packed (left unchanged). Synchronises. */
+int fw_batch_plan_autotune(fw_batch_plan* plan, const int32_t* d_packed, fw_stream_t stream);
+
+/* Solves every graph of the batch in place: one CUDA-graph launch (captured
+ * on the first call for this d_packed, replayed afterwards). */
+int fw_apsp_batched_i32(fw_batch_plan* plan, int32_t* d_packed, fw_stream_t stream);
+
+/* The chosen schedule as text, and the batch's total relaxations (sum n^3). */
+int fw_batch_plan_describe(const fw_batch_plan* plan, char* buf, size_t cap, double* relaxations);
+
+void fw_batch_plan_destroy(fw_batch_plan* plan);
+
 /* ---------------------------------------------------------------- host side */
 
 /* The reference's random digraph (src/graph_generator.cpp:7-46) into a host
