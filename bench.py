@@ -65,6 +65,7 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-graphs measurement")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable fp32 measurement")
     return ap.parse_args()
 
 
@@ -275,6 +276,10 @@ def run_ours(args) -> None:
     if not args.no_batched:
         batched = run_batched(args, F, torch, stream, world)
 
+    diff = None
+    if not args.no_diff:
+        diff = run_diff(args, torch, stream, world)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(h_in.numpy(), threads=1, seconds=args.cpu_seconds)
@@ -294,7 +299,7 @@ def run_ours(args) -> None:
             "gpu_launches": launches,
             "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()},
             "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary(),
-            "batched": batched,
+            "batched": batched, "differentiable": diff,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -346,6 +351,50 @@ def run_batched(args, F, torch, stream, world) -> dict:
             "ms_per_step": 1e3 * t_batched, "schedule": schedule,
             "loop_plain_graphs_per_s": world * count / t_loop, "loop_plain_ms_per_step": 1e3 * t_loop,
             "speedup_vs_loop": t_loop / t_batched, "relaxations_per_step": relax}
+
+
+def run_diff(args, torch, stream, world) -> dict:
+    """256 graphs at n = 256 (one batched call) plus one graph at n = 4096,
+    density 0.3, fp32 weights U(0.5, 10) tie-free, dL/dD ~ N(0, 1): forward
+    (distances + next hops) alone, and forward + backward, per step."""
+    from fw_cuda_gb300 import autograd as A
+    from fw_cuda_gb300 import workloads
+
+    rng = np.random.default_rng(5)
+    Wb = torch.from_numpy(np.stack([workloads.diff_graph(256, rng) for _ in range(256)])).cuda()
+    Wl = torch.from_numpy(workloads.diff_graph(4096, rng)).cuda()
+    Gb = torch.randn(Wb.shape, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    Gl = torch.randn(Wl.shape, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
+
+    def fwd():
+        A.forward_with_next_hops(Wb, stream)
+        A.forward_with_next_hops(Wl, stream)
+
+    def fwd_bwd():
+        _, nhb = A.forward_with_next_hops(Wb, stream)
+        _, nhl = A.forward_with_next_hops(Wl, stream)
+        A.backward_from_next_hops(Gb, nhb, stream)
+        A.backward_from_next_hops(Gl, nhl, stream)
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(a.elapsed_time(b) / 1e3, world) / args.steps
+
+    t_f = timed(fwd)
+    t_fb = timed(fwd_bwd)
+    relax = 256 * 256.0 ** 3 + 4096.0 ** 3
+    return {"workload": "256 graphs n=256 + 1 graph n=4096, density 0.3, fp32 U(0.5,10) tie-free, dL/dD ~ N(0,1)",
+            "forward_ms": 1e3 * t_f, "forward_backward_ms": 1e3 * t_fb, "fwd_bwd_over_fwd": t_fb / t_f,
+            "forward_relax_per_s": world * relax / t_f}
 
 
 def cpu_sample(W: np.ndarray, threads: int, seconds: float) -> dict:

@@ -181,6 +181,25 @@ int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_st
     return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, ws, need, stream);
 }
 
+int fw_forward_f32(float* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream) {
+    if (!d_D || !d_nh) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_forward_f32: NULL pointer");
+    if (n < 1 || n > 65535 || batch < 1 || batch > 65535)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_forward_f32: need 1 <= n <= 65535 and 1 <= batch <= 65535");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t need = f32_workspace_bytes(n, batch);
+    void* ws = workspace_get(s, need);
+    if (!ws) return FW_ERR_NO_MEMORY;
+    return f32_forward(d_D, d_nh, n, batch, ws, s);
+}
+
+int fw_backward(const float* d_dLdD, const int32_t* d_nh, float* d_dLdW, int64_t n, int64_t batch,
+                int32_t* d_bad_walks, fw_stream_t stream) {
+    if (!d_dLdD || !d_nh || !d_dLdW) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_backward: NULL pointer");
+    if (n < 1 || n > 16384 || batch < 1 || batch > 65535)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_backward: need 1 <= n <= 16384 and 1 <= batch <= 65535");
+    return f32_backward(d_dLdD, d_nh, d_dLdW, n, batch, d_bad_walks, reinterpret_cast<cudaStream_t>(stream));
+}
+
 int fw_generate_graph_i32(int32_t* h_out, int64_t n, double density, uint32_t seed, int32_t wmin, int32_t wmax) {
     if (h_out == nullptr) return set_error(FW_ERR_INVALID_ARGUMENT, "h_out is NULL");
     if (n < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "n must be >= 1");

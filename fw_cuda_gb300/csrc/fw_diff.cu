@@ -1,0 +1,433 @@
+// Differentiable Floyd-Warshall: an fp32 forward that also records next hops,
+// and a backward that scatters dL/dD onto the edge weights along the
+// recorded shortest paths. No reference counterpart (the reference is int32
+// only); the forward's relaxation and next-hop rule are those of the FP64
+// oracle sweep: if (D[i][k] + D[k][j] < D[i][j]) { D[i][j] = D[i][k] + D[k][j];
+// nh[i][j] = nh[i][k]; }, with missing edges +inf and nh[i][j] = j for an
+// edge, i on the diagonal, -1 for no edge.
+//
+// The forward is the same blocked schedule as the int32 engine — closed
+// 128 x 128 diagonal block, row / column panels as min-plus products with
+// that closure, then the remainder — on batches of equal-size graphs
+// (blockIdx.z = graph). Tiles are 128 x 128 on 512-thread CTAs (an 8 x 4
+// value + next-hop register micro-tile per thread); the remainder streams a
+// value slab and a next-hop slab of the transposed column panel plus a value
+// slab of the row panel per 32 pivots through a two-stage cp.async ring.
+//
+// Backward, per graph and destination j: the next hops toward j form a tree
+// rooted at j, and edge (u, nh[u][j]) lies on the path i -> j exactly when u
+// is on it, so dL/dW[u][nh[u][j]] += sum of dL/dD[i][j] over the sources i
+// whose path passes through u. One CTA per (destination, graph) walks every
+// source's path, accumulating those sums in shared memory, then adds them
+// into dL/dW. A walk that does not reach j within n hops is counted in a
+// status word instead of looping.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+
+#include "fw_common.cuh"
+#include "fw_internal.h"
+
+namespace fw {
+namespace {
+
+constexpr int kFThreads = 512;  // 16 row groups x 32 column groups
+constexpr int kFStages = 2;
+constexpr int kFSlabInts = kSlab * kTile;
+constexpr int kFStageInts = 3 * kFSlabInts;  // A values, A next hops, B values
+constexpr int kFSmemBytes = kFStages * kFStageInts * 4;  // 96 KB
+
+// Thread (tx = t % 32, ty = t / 32) of a 128 x 128 tile owns rows
+// own_row(ty, r), r < 8, and columns tx*4 .. tx*4+3.
+__device__ __forceinline__ void relax_nh(float& c, int& h, float a, int ha, float b) {
+    const float s = a + b;
+    if (s < c) {
+        c = s;
+        h = ha;
+    }
+}
+
+__device__ __forceinline__ float4 ld4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ int4 ld4i(const int* p) { return *reinterpret_cast<const int4*>(p); }
+
+// acc/nh for the 128 x 128 tile at (r0, c0) of an n x n matrix (inf / -1 outside).
+__device__ __forceinline__ void f_load_tile(float (&c)[8][4], int (&h)[8][4], const float* D, const int* nh,
+                                            int64_t n, int64_t r0, int64_t c0, int tx, int ty) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int64_t i = r0 + own_row(ty, r);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int64_t j = c0 + tx * 4 + e;
+            const bool in = i < n && j < n;
+            c[r][e] = in ? D[i * n + j] : INFINITY;
+            h[r][e] = in ? nh[i * n + j] : -1;
+        }
+    }
+}
+
+__device__ __forceinline__ void f_store_tile(const float (&c)[8][4], const int (&h)[8][4], float* D, int* nh, int64_t n,
+                                             int64_t r0, int64_t c0, int tx, int ty) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int64_t i = r0 + own_row(ty, r);
+        if (i >= n) continue;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int64_t j = c0 + tx * 4 + e;
+            if (j < n) {
+                D[i * n + j] = c[r][e];
+                nh[i * n + j] = h[r][e];
+            }
+        }
+    }
+}
+
+// Slab of a k-major workspace buffer (32 rows x 128 columns starting at c0).
+__device__ __forceinline__ void f_load_kmajor(void* dst, const void* buf, int64_t ldp, int k0, int64_t c0, int tid) {
+    for (int q = tid; q < kSlab * 32; q += kFThreads) {
+        const int row = q >> 5, ch = q & 31;
+        cp_async16(static_cast<int*>(dst) + row * kTile + ch * 4,
+                   static_cast<const int*>(buf) + (int64_t)(k0 + row) * ldp + c0 + ch * 4);
+    }
+}
+
+// Slab of D rows [r0, r0 + 32), columns [c0, c0 + 128) (inf outside).
+__device__ __forceinline__ void f_load_rows(float* dst, const float* D, int64_t n, int64_t r0, int64_t c0, int tid) {
+    for (int q = tid; q < kSlab * kTile; q += kFThreads) {
+        const int row = q >> 7, col = q & 127;
+        const int64_t i = r0 + row, j = c0 + col;
+        dst[row * kTile + col] = (i < n && j < n) ? D[i * n + j] : INFINITY;
+    }
+}
+
+// Transposed slab of D and nh: dst[kk][i] = X[r0 + i][k0 + kk].
+__device__ __forceinline__ void f_load_transposed(float* dv, int* dh, const float* D, const int* nh, int64_t n,
+                                                  int64_t r0, int64_t k0, int tid) {
+    for (int q = tid; q < kTile * kSlab; q += kFThreads) {
+        const int i = q >> 5, kk = q & 31;
+        const int64_t gi = r0 + i, gk = k0 + kk;
+        const bool in = gi < n && gk < n;
+        dv[kk * kTile + i] = in ? D[gi * n + gk] : INFINITY;
+        dh[kk * kTile + i] = in ? nh[gi * n + gk] : -1;
+    }
+}
+
+// One slab: c/h = relax with A (values av, hops ah; k-major) and B (bv; k-major).
+__device__ __forceinline__ void f_relax_slab(float (&c)[8][4], int (&h)[8][4], const float* av, const int* ah,
+                                             const float* bv, int nk, int tx, int ty) {
+#pragma unroll 2
+    for (int kk = 0; kk < nk; ++kk) {
+        const float4 a0 = ld4f(av + kk * kTile + ty * 4), a1 = ld4f(av + kk * kTile + 64 + ty * 4);
+        const int4 h0 = ld4i(ah + kk * kTile + ty * 4), h1 = ld4i(ah + kk * kTile + 64 + ty * 4);
+        const float4 b = ld4f(bv + kk * kTile + tx * 4);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const int ha[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+        const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) relax_nh(c[r][e], h[r][e], a[r], ha[r], bb[e]);
+    }
+}
+
+// Two-stage pipeline over the pivot slabs: la(av, ah, s) / lb(bv, s) fill slab s.
+template <class LA, class LB>
+__device__ __forceinline__ void f_mainloop(float (&c)[8][4], int (&h)[8][4], int kv, int* smem, LA la, LB lb, int tx,
+                                           int ty) {
+    const int nslab = (kv + kSlab - 1) / kSlab;
+    auto stage = [&](int s) { return smem + (s % kFStages) * kFStageInts; };
+    {
+        int* st = stage(0);
+        la(reinterpret_cast<float*>(st), st + kFSlabInts, 0);
+        lb(reinterpret_cast<float*>(st + 2 * kFSlabInts), 0);
+        cp_async_commit();
+    }
+    for (int s = 0; s < nslab; ++s) {
+        if (s + 1 < nslab) {
+            int* st = stage(s + 1);
+            la(reinterpret_cast<float*>(st), st + kFSlabInts, s + 1);
+            lb(reinterpret_cast<float*>(st + 2 * kFSlabInts), s + 1);
+        }
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();
+        const int* st = stage(s);
+        const int nk = min(kSlab, kv - s * kSlab);
+        f_relax_slab(c, h, reinterpret_cast<const float*>(st), st + kFSlabInts,
+                     reinterpret_cast<const float*>(st + 2 * kFSlabInts), nk, tx, ty);
+        __syncthreads();
+    }
+}
+
+// Next hops of the input: j for an edge, i on the diagonal, -1 otherwise.
+__global__ void fw_nh_init_kernel(const float* __restrict__ D, int* __restrict__ nh, int64_t n, int64_t total) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = q % (n * n);
+        const int64_t i = e / n, j = e % n;
+        nh[q] = (i == j) ? (int)i : (isfinite(D[q]) ? (int)j : -1);
+    }
+}
+
+// Phase 1: closure of the diagonal block of graph blockIdx.z; 512 threads,
+// 4 x 8 values + next hops each; also fills the workspace panels.
+__global__ void __launch_bounds__(kFThreads, 1)
+    fw_f32_diag_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int64_t p0,
+                       float* __restrict__ colTall, int* __restrict__ colHall, float* __restrict__ rowPall) {
+    __shared__ __align__(16) float prow[2][kTile];
+    __shared__ __align__(16) float pcol[2][kTile];
+    __shared__ __align__(16) int pcolh[2][kTile];
+    const int64_t gph = blockIdx.z;
+    float* D = Dall + gph * n * n;
+    int* nh = nhall + gph * n * n;
+    float* colT = colTall + gph * kTile * ldp;
+    int* colH = colHall + gph * kTile * ldp;
+    float* rowP = rowPall + gph * kTile * ldp;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;  // rows ty*4.., columns tx*8..
+    float c[4][8];
+    int h[4][8];
+    const int64_t rem = n - p0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int lr = ty * 4 + r, lc = tx * 8 + e;
+            const bool in = lr < rem && lc < rem;
+            c[r][e] = in ? D[(p0 + lr) * n + p0 + lc] : INFINITY;
+            h[r][e] = in ? nh[(p0 + lr) * n + p0 + lc] : -1;
+        }
+    if (ty == 0)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) prow[0][tx * 8 + e] = c[0][e];
+    if (tx == 0)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            pcol[0][ty * 4 + r] = c[r][0];
+            pcolh[0][ty * 4 + r] = h[r][0];
+        }
+    __syncthreads();
+    for (int kb = 0; kb < kTile; kb += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int k = kb + u, buf = u & 1;
+            float a[4], b[8];
+            int ha[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                a[r] = pcol[buf][ty * 4 + r];
+                ha[r] = pcolh[buf][ty * 4 + r];
+            }
+#pragma unroll
+            for (int e = 0; e < 8; ++e) b[e] = prow[buf][tx * 8 + e];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int e = 0; e < 8; ++e) relax_nh(c[r][e], h[r][e], a[r], ha[r], b[e]);
+            const int k1 = k + 1;
+            if (k1 < kTile) {
+                const int sr = (u + 1) & 3, sc = (u + 1) & 7;
+                if (ty == (k1 >> 2))
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) prow[buf ^ 1][tx * 8 + e] = c[sr][e];
+                if (tx == (k1 >> 3))
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        pcol[buf ^ 1][ty * 4 + r] = c[r][sc];
+                        pcolh[buf ^ 1][ty * 4 + r] = h[r][sc];
+                    }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int lr = ty * 4 + r, lc = tx * 8 + e;
+            if (lr < rem && lc < rem) {
+                D[(p0 + lr) * n + p0 + lc] = c[r][e];
+                nh[(p0 + lr) * n + p0 + lc] = h[r][e];
+            }
+            colT[(int64_t)lc * ldp + p0 + lr] = c[r][e];
+            colH[(int64_t)lc * ldp + p0 + lr] = h[r][e];
+            rowP[(int64_t)lr * ldp + p0 + lc] = c[r][e];
+        }
+}
+
+// Phase 2: blockIdx.y == 0 -> row panel tile (P, J); == 1 -> column panel tile (I, P).
+__global__ void __launch_bounds__(kFThreads, 1)
+    fw_f32_panel_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
+                        float* __restrict__ colTall, int* __restrict__ colHall, float* __restrict__ rowPall) {
+    extern __shared__ __align__(128) int smem[];
+    const int64_t gph = blockIdx.z;
+    float* D = Dall + gph * n * n;
+    int* nh = nhall + gph * n * n;
+    float* colT = colTall + gph * kTile * ldp;
+    int* colH = colHall + gph * kTile * ldp;
+    float* rowP = rowPall + gph * kTile * ldp;
+    const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    const int other = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
+    const int64_t p0 = (int64_t)pt * kTile, q0 = (int64_t)other * kTile;
+    const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
+    float c[8][4];
+    int h[8][4];
+    if (blockIdx.y == 0) {
+        f_load_tile(c, h, D, nh, n, p0, q0, tx, ty);
+        f_mainloop(
+            c, h, kv, smem,
+            [&](float* av, int* ah, int s) {
+                f_load_kmajor(av, colT, ldp, s * kSlab, p0, tid);
+                f_load_kmajor(ah, colH, ldp, s * kSlab, p0, tid);
+            },
+            [&](float* bv, int s) { f_load_rows(bv, D, n, p0 + s * kSlab, q0, tid); }, tx, ty);
+        f_store_tile(c, h, D, nh, n, p0, q0, tx, ty);
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) rowP[(int64_t)own_row(ty, r) * ldp + q0 + tx * 4 + e] = c[r][e];
+    } else {
+        f_load_tile(c, h, D, nh, n, q0, p0, tx, ty);
+        f_mainloop(
+            c, h, kv, smem,
+            [&](float* av, int* ah, int s) { f_load_transposed(av, ah, D, nh, n, q0, p0 + s * kSlab, tid); },
+            [&](float* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, p0, tid); }, tx, ty);
+        f_store_tile(c, h, D, nh, n, q0, p0, tx, ty);
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                colT[(int64_t)(tx * 4 + e) * ldp + q0 + own_row(ty, r)] = c[r][e];
+                colH[(int64_t)(tx * 4 + e) * ldp + q0 + own_row(ty, r)] = h[r][e];
+            }
+    }
+}
+
+// Phase 3: remainder tile (I, J) of graph blockIdx.z.
+__global__ void __launch_bounds__(kFThreads, 1)
+    fw_f32_remainder_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
+                            const float* __restrict__ colTall, const int* __restrict__ colHall,
+                            const float* __restrict__ rowPall) {
+    extern __shared__ __align__(128) int smem[];
+    const int64_t gph = blockIdx.z;
+    float* D = Dall + gph * n * n;
+    int* nh = nhall + gph * n * n;
+    const float* colT = colTall + gph * kTile * ldp;
+    const int* colH = colHall + gph * kTile * ldp;
+    const float* rowP = rowPall + gph * kTile * ldp;
+    const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
+    const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
+    const int64_t p0 = (int64_t)pt * kTile, r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
+    const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
+    float c[8][4];
+    int h[8][4];
+    f_load_tile(c, h, D, nh, n, r0, c0, tx, ty);
+    f_mainloop(
+        c, h, kv, smem,
+        [&](float* av, int* ah, int s) {
+            f_load_kmajor(av, colT, ldp, s * kSlab, r0, tid);
+            f_load_kmajor(ah, colH, ldp, s * kSlab, r0, tid);
+        },
+        [&](float* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, c0, tid); }, tx, ty);
+    f_store_tile(c, h, D, nh, n, r0, c0, tx, ty);
+}
+
+// Backward: CTA (j, graph). Shared: next hops toward j, dL/dD[:, j], path sums.
+__global__ void __launch_bounds__(256)
+    fw_backward_kernel(const float* __restrict__ Gall, const int* __restrict__ nhall, float* __restrict__ dWall,
+                       int64_t n, int* __restrict__ bad_walks) {
+    extern __shared__ __align__(16) int bsm[];
+    int* hop = bsm;                                        // n
+    float* gcol = reinterpret_cast<float*>(bsm + n);       // n
+    float* acc = reinterpret_cast<float*>(bsm + 2 * n);    // n
+    const int64_t gph = blockIdx.y;
+    const int64_t j = blockIdx.x;
+    const float* G = Gall + gph * n * n;
+    const int* nh = nhall + gph * n * n;
+    float* dW = dWall + gph * n * n;
+    for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+        hop[u] = nh[u * n + j];
+        gcol[u] = G[u * n + j];
+        acc[u] = 0.f;
+    }
+    __syncthreads();
+    int bad = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        if (i == j || hop[i] < 0) continue;
+        const float g = gcol[i];
+        int64_t u = i, steps = 0;
+        while (u != j && steps < n) {
+            atomicAdd(&acc[u], g);
+            const int v = hop[u];
+            if (v < 0 || v >= n) break;
+            u = v;
+            ++steps;
+        }
+        if (u != j) ++bad;
+    }
+    if (bad && bad_walks) atomicAdd(bad_walks, bad);
+    __syncthreads();
+    for (int64_t u = threadIdx.x; u < n; u += blockDim.x) {
+        const int v = hop[u];
+        if (u == j || v < 0 || v >= n) continue;
+        const float s = acc[u];
+        if (s != 0.f) atomicAdd(&dW[u * n + v], s);
+    }
+}
+
+}  // namespace
+
+size_t f32_workspace_bytes(int64_t n, int64_t batch) {
+    const int64_t ldp = (n + kTile - 1) / kTile * kTile;
+    return (size_t)3 * kTile * ldp * 4 * (size_t)batch;
+}
+
+int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
+    static bool attr_done = false;
+    if (!attr_done) {
+        FW_CUDA_TRY(cudaFuncSetAttribute(fw_f32_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+        FW_CUDA_TRY(
+            cudaFuncSetAttribute(fw_f32_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+        attr_done = true;
+    }
+    const int T = (int)((n + kTile - 1) / kTile);
+    const int64_t ldp = (int64_t)T * kTile;
+    float* colT = static_cast<float*>(ws);
+    int* colH = reinterpret_cast<int*>(colT + (size_t)kTile * ldp * batch);
+    float* rowP = reinterpret_cast<float*>(colH + (size_t)kTile * ldp * batch);
+    const int64_t total = n * n * batch;
+    prof_begin(KC_FWD_F32, s);
+    fw_nh_init_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 4096), 256, 0, s>>>(D, nh, n, total);
+    FW_LAUNCH_CHECK("fw_nh_init_kernel");
+    for (int pt = 0; pt < T; ++pt) {
+        const int64_t p0 = (int64_t)pt * kTile;
+        fw_f32_diag_kernel<<<dim3(1, 1, (unsigned)batch), kFThreads, 0, s>>>(D, nh, n, ldp, p0, colT, colH, rowP);
+        FW_LAUNCH_CHECK("fw_f32_diag_kernel");
+        if (T > 1) {
+            fw_f32_panel_kernel<<<dim3(T - 1, 2, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(D, nh, n, ldp, pt,
+                                                                                             colT, colH, rowP);
+            FW_LAUNCH_CHECK("fw_f32_panel_kernel");
+            fw_f32_remainder_kernel<<<dim3(T - 1, T - 1, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(
+                D, nh, n, ldp, pt, colT, colH, rowP);
+            FW_LAUNCH_CHECK("fw_f32_remainder_kernel");
+        }
+    }
+    prof_end(KC_FWD_F32, s, (double)n * n * n * batch);
+    return FW_OK;
+}
+
+int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s) {
+    FW_CUDA_TRY(cudaMemsetAsync(dW, 0, sizeof(float) * (size_t)(n * n * batch), s));
+    const size_t smem = (size_t)3 * n * 4;
+    if (smem > 48 * 1024) {
+        FW_CUDA_TRY(cudaFuncSetAttribute(fw_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    prof_begin(KC_BWD_F32, s);
+    fw_backward_kernel<<<dim3((unsigned)n, (unsigned)batch), 256, smem, s>>>(G, nh, dW, n, d_bad);
+    FW_LAUNCH_CHECK("fw_backward_kernel");
+    prof_end(KC_BWD_F32, s, (double)n * n * batch);
+    return FW_OK;
+}
+
+}  // namespace fw

@@ -60,6 +60,11 @@ int blocked_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 size_t pivot_workspace_bytes(int64_t n);
 int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 
+// Differentiable fp32 forward / backward (fw_diff.cu).
+size_t f32_workspace_bytes(int64_t n, int64_t batch);
+int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
+int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s);
+
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);
 

@@ -112,6 +112,24 @@ int fw_batch_plan_describe(const fw_batch_plan* plan, char* buf, size_t cap, dou
 
 void fw_batch_plan_destroy(fw_batch_plan* plan);
 
+/* ---------------------------------------------------------------- differentiable */
+
+/* fp32 APSP that also records next hops, for `batch` graphs of n x n stored
+ * one after another (stride n*n). No counterpart in the reference. On entry
+ * d_D holds the weights (+inf = no edge); on return the distances, and d_nh
+ * the next hop of every shortest path (nh[i][j] = j for a direct edge, i on
+ * the diagonal, -1 when j is unreachable), updated as in the sweep
+ * if (D[i][k] + D[k][j] < D[i][j]) { D[i][j] = D[i][k] + D[k][j]; nh[i][j] = nh[i][k]; }. */
+int fw_forward_f32(float* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream);
+
+/* dL/dW for L depending on D = fw_forward_f32(W): every edge (u, v) on the
+ * recorded path i -> j receives dL/dD[i][j]; d_dLdW is overwritten (zero for
+ * non-edges). d_bad_walks, if not NULL, is a device int incremented by the
+ * number of paths that did not reach their end within n hops (0 for a valid
+ * next-hop matrix). Floating-point atomics: the summation order varies. */
+int fw_backward(const float* d_dLdD, const int32_t* d_nh, float* d_dLdW, int64_t n, int64_t batch,
+                int32_t* d_bad_walks, fw_stream_t stream);
+
 /* ---------------------------------------------------------------- host side */
 
 /* The reference's random digraph (src/graph_generator.cpp:7-46) into a host
