@@ -30,6 +30,7 @@
 // taken by the previous launch, so no launch reads what it writes.
 #include <cstdio>
 #include <cstdlib>
+#include <utility>
 
 #include "fw_common.cuh"
 #include "fw_internal.h"
@@ -133,22 +134,35 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// Phase 3: tile (I, J), both different from the pivot tile:
-// D[I][J] = min(D[I][J], colT[:, I]^T (x) rowP[:, J]).
+// Tile index sets of the remainder launches: either every tile index except
+// up to two excluded ones (ex0 < ex1, -1 = none), or one single index.
+struct TileSet {
+    int single;  // >= 0: the only index; -1: all but the excluded ones
+    int ex0, ex1;
+};
+
+__device__ __forceinline__ int tile_of(const TileSet& s, int idx) {
+    if (s.single >= 0) return s.single;
+    if (s.ex0 >= 0 && idx >= s.ex0) ++idx;
+    if (s.ex1 >= 0 && idx >= s.ex1) ++idx;
+    return idx;
+}
+
+// Phase 3: tiles (I, J), I from `rows`, J from `cols`:
+// D[I][J] = min(D[I][J], colT[k][I]^T (x) rowP[k][J]) over workspace pivot
+// rows k in [slab0 * 32, (slab0 + nslab) * 32).
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
-    fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int pt, int nslab,
+    fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, TileSet cols, int slab0, int nslab,
                         const int* __restrict__ colT, const int* __restrict__ rowP, int one) {
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
-    const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
-    const int64_t r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
+    const int64_t r0 = (int64_t)tile_of(rows, blockIdx.y) * kTile, c0 = (int64_t)tile_of(cols, blockIdx.x) * kTile;
     int acc[8][8];
     load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
     mainloop<kMixA>(
-        acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, s * kSlab, r0, tid); },
-        [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, c0, tid); }, tx, ty, one);
+        acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, (slab0 + s) * kSlab, r0, tid); },
+        [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, (slab0 + s) * kSlab, c0, tid); }, tx, ty, one);
     store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
 }
 
@@ -201,8 +215,101 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+TileSet all_but(int a, int b = -1) {
+    if (b >= 0 && b < a) std::swap(a, b);
+    if (a < 0) std::swap(a, b);
+    return TileSet{-1, a, b};
+}
+TileSet only(int t) { return TileSet{t, -1, -1}; }
+
 template <bool VEC>
-int blocked_solve_impl(int32_t* D, int64_t n, int* colT, int* rowP, cudaStream_t s) {
+struct Blocked {
+    int32_t* D;
+    int64_t n, ldp;
+    int T;
+    int* colT;  // [rows_per_pass][ldp]
+    int* rowP;
+    cudaStream_t s;
+
+    int64_t p0(int t) const { return (int64_t)t * kTile; }
+    int64_t kv(int t) const { return n - p0(t) < kTile ? n - p0(t) : kTile; }
+
+    // Diagonal closure of block t, its panels written to workspace half h.
+    int diag(int t, int h) {
+        prof_begin(KC_DIAG, s);
+        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, s>>>(D, n, ldp, p0(t), colT + h * kTile * ldp, rowP + h * kTile * ldp);
+        FW_LAUNCH_CHECK("fw_diag_kernel");
+        prof_end(KC_DIAG, s, (double)kv(t) * kv(t) * kv(t));
+        return FW_OK;
+    }
+    int panels(int t, int h) {
+        if (T < 2) return FW_OK;
+        const int nslab = (int)((kv(t) + kSlab - 1) / kSlab);
+        prof_begin(KC_PANEL, s);
+        fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, t, nslab, colT + h * kTile * ldp,
+                                                                         rowP + h * kTile * ldp, 1);
+        FW_LAUNCH_CHECK("fw_panel_kernel");
+        prof_end(KC_PANEL, s, 2.0 * (double)(n - kv(t)) * kv(t) * kv(t));
+        return FW_OK;
+    }
+    // Remainder launch over rows x cols with pivots [k_begin, k_end) of the
+    // workspace (k_end - k_begin valid pivots; slabs rounded up).
+    int remainder(TileSet rows, int nrows, TileSet cols, int ncols, int k_begin, int k_valid) {
+        if (nrows <= 0 || ncols <= 0 || k_valid <= 0) return FW_OK;
+        const int slab0 = k_begin / kSlab;
+        const int nslab = (k_valid + kSlab - 1) / kSlab;
+        prof_begin(KC_REMAINDER, s);
+        fw_remainder_kernel<VEC><<<dim3(ncols, nrows), kThreads, kSmemBytes, s>>>(D, n, ldp, rows, cols, slab0, nslab,
+                                                                                 colT, rowP, 1);
+        FW_LAUNCH_CHECK("fw_remainder_kernel");
+        prof_end(KC_REMAINDER, s, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
+        return FW_OK;
+    }
+    // Number of matrix rows (or columns) the tile set covers.
+    double relax_of(const TileSet& ts, int count) const {
+        (void)count;
+        if (ts.single >= 0) return (double)kv(ts.single);
+        double r = (double)n;
+        if (ts.ex0 >= 0) r -= (double)kv(ts.ex0);
+        if (ts.ex1 >= 0) r -= (double)kv(ts.ex1);
+        return r;
+    }
+
+    // One 128-wide pivot block per remainder pass (tiling_gpu; kappa <= 4).
+    int single(int t) {
+        if (int rc = diag(t, 0)) return rc;
+        if (int rc = panels(t, 0)) return rc;
+        return remainder(all_but(t), T - 1, all_but(t), T - 1, 0, (int)kv(t));
+    }
+
+    // Two pivot blocks t1 = t, t2 = t + 1 folded into one remainder pass of
+    // 256 pivots (kappa >= 5). With C1/R1 the panels of block 1 after block 1
+    // and C2/R2 those of block 2 after both blocks, the final value of a tile
+    // outside both blocks' rows and columns is min(D, C1 (x) R1, C2 (x) R2):
+    //   1. close block 1, its panels -> workspace half 0 (C1, R1)
+    //   2. block 1's update of block 2's row and column (the tiles block 2
+    //      needs before it can be closed)
+    //   3. close block 2, its panels -> workspace half 1 (C2, R2)
+    //   4. the remainder: all other tiles, 256 pivots from both halves
+    //   5. block 2's update of block 1's row and column (the panels of
+    //      block 1 were final only with respect to block 1).
+    int pair(int t) {
+        const int t1 = t, t2 = t + 1;
+        const int k1 = (int)kv(t1), k2 = (int)kv(t2);
+        if (int rc = diag(t1, 0)) return rc;
+        if (int rc = panels(t1, 0)) return rc;
+        if (int rc = remainder(only(t2), 1, all_but(t1), T - 1, 0, k1)) return rc;
+        if (int rc = remainder(all_but(t1, t2), T - 2, only(t2), 1, 0, k1)) return rc;
+        if (int rc = diag(t2, 1)) return rc;
+        if (int rc = panels(t2, 1)) return rc;
+        if (int rc = remainder(all_but(t1, t2), T - 2, all_but(t1, t2), T - 2, 0, kTile + k2)) return rc;
+        if (int rc = remainder(only(t1), 1, all_but(t2), T - 1, kTile, k2)) return rc;
+        return remainder(all_but(t1, t2), T - 2, only(t1), 1, kTile, k2);
+    }
+};
+
+template <bool VEC>
+int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, int* rowP, cudaStream_t s) {
     static bool attr_done = false;
     if (!attr_done) {
         FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
@@ -210,27 +317,15 @@ int blocked_solve_impl(int32_t* D, int64_t n, int* colT, int* rowP, cudaStream_t
             cudaFuncSetAttribute(fw_remainder_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
         attr_done = true;
     }
-    const int T = (int)((n + kTile - 1) / kTile);
-    const int64_t ldp = (int64_t)T * kTile;
-    const int one = 1;
-    for (int pt = 0; pt < T; ++pt) {
-        const int64_t p0 = (int64_t)pt * kTile;
-        const int64_t kv = n - p0 < kTile ? n - p0 : kTile;
-        const int nslab = (int)((kv + kSlab - 1) / kSlab);
-        prof_begin(KC_DIAG, s);
-        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, s>>>(D, n, ldp, p0, colT, rowP);
-        FW_LAUNCH_CHECK("fw_diag_kernel");
-        prof_end(KC_DIAG, s, (double)kv * kv * kv);
-        if (T > 1) {
-            prof_begin(KC_PANEL, s);
-            fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP, one);
-            FW_LAUNCH_CHECK("fw_panel_kernel");
-            prof_end(KC_PANEL, s, 2.0 * (double)(n - kv) * kv * kv);
-            prof_begin(KC_REMAINDER, s);
-            fw_remainder_kernel<VEC>
-                <<<dim3(T - 1, T - 1), kThreads, kSmemBytes, s>>>(D, n, ldp, pt, nslab, colT, rowP, one);
-            FW_LAUNCH_CHECK("fw_remainder_kernel");
-            prof_end(KC_REMAINDER, s, (double)(n - kv) * (n - kv) * kv);
+    Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s};
+    b.ldp = (int64_t)b.T * kTile;
+    for (int t = 0; t < b.T;) {
+        if (blocks_per_pass == 2 && t + 1 < b.T) {
+            if (int rc = b.pair(t)) return rc;
+            t += 2;
+        } else {
+            if (int rc = b.single(t)) return rc;
+            t += 1;
         }
     }
     return FW_OK;
@@ -238,17 +333,24 @@ int blocked_solve_impl(int32_t* D, int64_t n, int* colT, int* rowP, cudaStream_t
 
 }  // namespace
 
-size_t blocked_workspace_bytes(int64_t n) {
-    const int64_t T = (n + kTile - 1) / kTile;
-    return (size_t)2 * kTile * (size_t)(T * kTile) * sizeof(int);
+int blocks_per_pass(int variant, int kappa) {
+    // The reference's kappa counts 32-wide tiles per pass; 128-wide blocks
+    // cover kappa <= 4, two blocks (256 pivots) cover the larger values.
+    return (variant == FW_VARIANT_MULTI_LAYER && normalise_kappa(kappa) > 4) ? 2 : 1;
 }
 
-int blocked_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
+size_t blocked_workspace_bytes(int64_t n, int blocks) {
+    const int64_t T = (n + kTile - 1) / kTile;
+    return (size_t)2 * blocks * kTile * (size_t)(T * kTile) * sizeof(int);
+}
+
+int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, cudaStream_t s) {
     const int64_t T = (n + kTile - 1) / kTile;
     int* colT = static_cast<int*>(ws);
-    int* rowP = colT + (size_t)kTile * (size_t)(T * kTile);
+    int* rowP = colT + (size_t)blocks * kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    return vec ? blocked_solve_impl<true>(D, n, colT, rowP, s) : blocked_solve_impl<false>(D, n, colT, rowP, s);
+    return vec ? blocked_solve_impl<true>(D, n, blocks, colT, rowP, s)
+               : blocked_solve_impl<false>(D, n, blocks, colT, rowP, s);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }

@@ -151,15 +151,13 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     (void)kappa;
     if (n < 1) return 0;
     if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
-    return blocked_workspace_bytes(n);
+    return blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
 }
 
 int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
                    size_t workspace_bytes, fw_stream_t stream) {
     if (int rc = check_apsp_args(d_D, n, variant)) return rc;
     (void)tile;  // fixed geometry, as in the reference (src/fw_tiling_gpu.cu:254-257)
-    kappa = normalise_kappa(kappa);
-    (void)kappa;
     const size_t need = fw_workspace_bytes_i32(n, tile, kappa, variant);
     if (d_workspace == nullptr || workspace_bytes < need)
         return set_error(FW_ERR_INVALID_ARGUMENT,
@@ -169,7 +167,7 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
         return set_error(FW_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
-    return blocked_solve(d_D, n, d_workspace, s);
+    return blocked_solve(d_D, n, blocks_per_pass(variant, kappa), d_workspace, s);
 }
 
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {

@@ -29,9 +29,10 @@ constexpr int kStageInts = 2 * kSlabInts;                // A slab + B slab
 constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 
 // Number of the 8 micro-tile columns that fold a pivot pair with two DPX
-// add-min instructions; the other columns use form B (see relax2). 3 of 8
-// balances the ALU and FMA pipes best on GB300 (measured).
-constexpr int kMixA = 3;
+// add-min instructions; the other columns use form B (see relax2). Measured on
+// GB300 in the remainder kernel (one launch, n = 16384): 8 of 8 (DPX only)
+// 1.78e13, 3 of 8 1.83e13, 5 of 8 1.86e13, 0 of 8 1.54e13 relaxations/s.
+constexpr int kMixA = 5;
 
 // Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
 // ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns

@@ -55,8 +55,9 @@ void* workspace_get(cudaStream_t s, size_t bytes);
 int normalise_kappa(int kappa);
 
 // Blocked-sweep launchers (fw_apsp_i32.cu).
-size_t blocked_workspace_bytes(int64_t n);
-int blocked_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
+int blocks_per_pass(int variant, int kappa);
+size_t blocked_workspace_bytes(int64_t n, int blocks);
+int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, cudaStream_t s);
 size_t pivot_workspace_bytes(int64_t n);
 int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 

@@ -65,6 +65,9 @@ int scratch_address(void** out) {
 
 extern "C" int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
                                    fw_stream_t stream) {
+    // The two-block schedule of kappa > 4 needs twice the panel workspace;
+    // kappa only selects the schedule, not the result, so cap it here.
+    if (kappa > 4) kappa = 4;
     if (n > kNoAllocMaxN)
         return fw::set_error(FW_ERR_INVALID_ARGUMENT,
                              "fw_apsp_i32_noalloc: n = " + std::to_string(n) +

@@ -88,17 +88,19 @@ int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s) {
     FW_CUDA_TRY(cudaMemsetAsync(in, 0, 768 * sizeof(int), s));
     // MIXA = 8: every pair as two DPX add-mins. The others: the remainder's
     // mix (kMixA) and its neighbours; the best of all is the ceiling.
-    double r8 = 0, r2 = 0, r3 = 0, r4 = 0;
+    double r8 = 0, r2 = 0, r3 = 0, r4 = 0, r5 = 0;
     int rc = time_peak<8>(blocks, in, out, s, &r8);
     if (!rc) rc = time_peak<2>(blocks, in, out, s, &r2);
     if (!rc) rc = time_peak<3>(blocks, in, out, s, &r3);
     if (!rc) rc = time_peak<4>(blocks, in, out, s, &r4);
+    if (!rc) rc = time_peak<5>(blocks, in, out, s, &r5);
     cudaFreeAsync(in, s);
     cudaFreeAsync(out, s);
     if (rc) return rc;
     if (dpx_only) *dpx_only = r8;
     double best = r2 > r3 ? r2 : r3;
     best = best > r4 ? best : r4;
+    best = best > r5 ? best : r5;
     best = best > r8 ? best : r8;
     if (mixed) *mixed = best;
     return FW_OK;

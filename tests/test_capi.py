@@ -67,6 +67,9 @@ def test_workspace_sizes(fw):
     assert fw.workspace_bytes_i32(1, variant=1) == 2 * 128 * 128 * 4
     assert fw.workspace_bytes_i32(32768, variant=2) == 2 * 128 * 32768 * 4
     assert fw.workspace_bytes_i32(32769, variant=2) == 2 * 128 * (32768 + 128) * 4
+    # kappa > 4: two 128-wide pivot blocks per remainder pass, twice the panels
+    assert fw.workspace_bytes_i32(32768, kappa=8, variant=2) == 2 * 256 * 32768 * 4
+    assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == 2 * 128 * 32768 * 4
     # per-pivot: two row and two column snapshots
     assert fw.workspace_bytes_i32(1001, variant=0) == 4 * 1004 * 4
     assert fw.workspace_bytes_i32(0, variant=1) == 0

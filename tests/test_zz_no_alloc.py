@@ -22,17 +22,17 @@ def _noalloc(fw):
     return f
 
 
-@pytest.mark.parametrize("n,variant", [(1000, 2), (8192, 2), (777, 1), (300, 0)])
-def test_noalloc_matches_allocating_entry_point_twice(fw, cuda, n, variant):
+@pytest.mark.parametrize("n,variant,kappa", [(1000, 2, 4), (8192, 2, 4), (8192, 2, 8), (777, 1, 4), (300, 0, 4)])
+def test_noalloc_matches_allocating_entry_point_twice(fw, cuda, n, variant, kappa):
     f = _noalloc(fw)
     W = fw.generate_graph(n, 0.3, 4242 + n, 1, 100)
     ref = cuda.from_numpy(W).cuda()
-    fw.apsp_i32(ref, n, 32, 4, variant, None)
+    fw.apsp_i32(ref, n, 32, kappa, variant, None)
     cuda.cuda.synchronize()
     expected = ref.cpu().numpy()
     for call in range(2):  # the second call sees the scratch the first one left behind
         d = cuda.from_numpy(W).cuda()
-        rc = f(d.data_ptr(), n, 32, 4, variant, None)
+        rc = f(d.data_ptr(), n, 32, kappa, variant, None)
         assert rc == fw.FW_OK, fw.lib().fw_last_error_string()
         cuda.cuda.synchronize()
         assert np.array_equal(d.cpu().numpy(), expected), (n, variant, call)
