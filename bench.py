@@ -44,7 +44,7 @@ UNIT = "relax/s"
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-VARIANTS = {"baseline_gpu": 0, "tiling_gpu": 1, "multi_layer_tiling_gpu": 2}
+VARIANTS = {"baseline_gpu": 0, "tiling_gpu": 1, "multi_layer_tiling_gpu": 2, "auto": 3}
 
 
 def parse() -> argparse.Namespace:
@@ -58,8 +58,11 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--wmin", type=int, default=1)
     ap.add_argument("--wmax", type=int, default=100)
-    ap.add_argument("--algorithm", default="multi_layer_tiling_gpu", choices=list(VARIANTS))
-    ap.add_argument("--kappa", type=int, default=4)
+    ap.add_argument("--algorithm", default="auto", choices=list(VARIANTS),
+                    help="auto = exact packed 16-bit sweep when provably identical, else multi_layer_tiling_gpu")
+    ap.add_argument("--kappa", type=int, default=8)
+    ap.add_argument("--no-int32", action="store_true",
+                    help="skip the extra timing of the int32 multi-layer sweep next to an auto run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -239,38 +242,36 @@ def run_ours(args) -> None:
         # exceeds its input edge weight.
         assert torch.all(torch.diagonal(work) == 0).item()
 
-    rem = prof.get("fw_remainder", {"launches": 0, "total_ms": 0.0, "relaxations": 0.0})
-    roofline = None
-    if rem["launches"]:
-        achieved = rem["relaxations"] / (rem["total_ms"] / 1e3)
-        # algorithmic bytes of one remainder launch: its tiles read + written once, plus
-        # the two 128-wide panels it streams (n' = n - 128 rows/columns outside the pivot block)
-        nr = n - 128
-        bytes_per_launch = 8.0 * nr * nr + 2.0 * 4 * 128 * nr
-        hbm_gbs = bytes_per_launch * rem["launches"] / (rem["total_ms"] / 1e3) / 1e9
-        peaks = {}
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                peaks = json.load(f)
-        except OSError:
-            pass
-        hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-        roofline = {
-            "kernel": "fw_remainder_kernel",
-            "bound": "int_issue",
-            "achieved": achieved,
-            "peak": peak_mixed,
-            "unit": UNIT,
-            "frac": achieved / peak_mixed,
-            "peak_source": "measured live: register-only relaxation kernels (fw_measure_relax_peak), best instruction mix",
-            "dpx_only_peak": peak_dpx,
-            "frac_of_dpx_only": achieved / peak_dpx,
-            "traffic": None,
-            "avg_launch_ms": rem["total_ms"] / rem["launches"],
-            "relax_per_launch": rem["relaxations"] / rem["launches"],
-            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback"},
-        }
+    used_packed = F.auto_used_packed(stream) if variant == VARIANTS["auto"] else False
+    peak_packed = F.measure_relax_peak_packed(stream) if used_packed else None
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    if used_packed:
+        roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, peak_packed,
+                               "measured live: register-only packed 16-bit DPX add-min kernel "
+                               "(fw_measure_relax_peak_packed)", hbm_peak, "hbm_gbs" in peaks)
+        if roofline:
+            roofline["int32_dpx_only_peak"] = peak_dpx
+    else:
+        roofline = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 128, 4, peak_mixed,
+                               "measured live: register-only relaxation kernels (fw_measure_relax_peak), "
+                               "best instruction mix", hbm_peak, "hbm_gbs" in peaks)
+        if roofline:
+            roofline["dpx_only_peak"] = peak_dpx
+            roofline["frac_of_dpx_only"] = roofline["achieved"] / peak_dpx
+            if args.kappa <= 4:
+                # ncu (profiles/fw_remainder_n8192.md): 468.4 MB of DRAM traffic per remainder
+                # launch at n = 8192 (63^2 tiles); traffic scales with the tiles a launch touches.
+                roofline["traffic"] = 468.4e6 * ((n - 128) / 8064.0) ** 2
+    int32_path = None
+    if variant == VARIANTS["auto"] and not args.no_int32:
+        int32_path = time_variant(F, torch, stream, work, pristine, n, args.kappa, VARIANTS["multi_layer_tiling_gpu"],
+                                  args.steps, world, relax)
 
     batched = None
     if not args.no_batched:
@@ -300,12 +301,57 @@ def run_ours(args) -> None:
             "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()},
             "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary(),
             "batched": batched, "differentiable": diff,
+            "path": ("packed16" if used_packed else "int32") if variant == VARIANTS["auto"] else "int32",
+            "int32_path": int32_path,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def roofline_of(stats, kernel, n, block, bytes_per_value, peak, peak_source, hbm_peak, hbm_measured):
+    """Roofline of the dominant kernel from its event-timed launches."""
+    if not stats or not stats["launches"]:
+        return None
+    secs = stats["total_ms"] / 1e3
+    achieved = stats["relaxations"] / secs
+    # algorithmic bytes of one remainder launch: its tiles read + written once,
+    # plus the two `block`-wide panels it streams (n' = n - block)
+    nr = n - block
+    bytes_per_launch = 2.0 * bytes_per_value * nr * nr + 2.0 * 4 * block * nr
+    hbm_gbs = bytes_per_launch * stats["launches"] / secs / 1e9
+    return {"kernel": kernel, "bound": "int_issue", "achieved": achieved, "peak": peak, "unit": UNIT,
+            "frac": achieved / peak, "peak_source": peak_source, "traffic": None,
+            "avg_launch_ms": stats["total_ms"] / stats["launches"],
+            "relax_per_launch": stats["relaxations"] / stats["launches"],
+            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm_measured else "fallback"}}
+
+
+def time_variant(F, torch, stream, work, pristine, n, kappa, variant, steps, world, relax) -> dict:
+    """The same restore + solve steps with another variant (one warm-up step)."""
+    def step():
+        work.copy_(pristine, non_blocking=True)
+        F.apsp_i32(work, n, 32, kappa, variant, stream)
+
+    step()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    F.profile_begin()
+    a.record(stream)
+    for _ in range(steps):
+        step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    prof = F.profile_end()
+    el = max_over_ranks(a.elapsed_time(b) / 1e3, world)
+    rem = prof.get("fw_remainder", {"launches": 0, "total_ms": 1.0, "relaxations": 0.0})
+    return {"algorithm": "multi_layer_tiling_gpu", "kappa": kappa, "value": aggregate(world, steps, relax, el),
+            "unit": UNIT, "ms_per_step": 1e3 * el / steps,
+            "remainder_relax_per_s": rem["relaxations"] / (rem["total_ms"] / 1e3)}
 
 
 def run_batched(args, F, torch, stream, world) -> dict:

@@ -34,6 +34,7 @@ FW_ERR_NOT_BUILT = 5
 VARIANT_BASELINE = 0
 VARIANT_TILING = 1
 VARIANT_MULTI_LAYER = 2
+VARIANT_AUTO = 3  # exact packed 16-bit sweep when provably identical, else the multi-layer int32 sweep
 
 # Every symbol include/fw103.h declares (checked by the CPU tests).
 EXPORTED_SYMBOLS = (
@@ -46,6 +47,8 @@ EXPORTED_SYMBOLS = (
     "fw_profile_begin",
     "fw_profile_end",
     "fw_measure_relax_peak",
+    "fw_apsp_auto_report",
+    "fw_measure_relax_peak_packed",
     "fw_batch_pack_offsets",
     "fw_batch_plan_create",
     "fw_batch_plan_autotune",
@@ -108,6 +111,10 @@ def lib():
     L.fw_profile_end.restype = c_int
     L.fw_measure_relax_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak.restype = c_int
+    L.fw_measure_relax_peak_packed.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
+    L.fw_measure_relax_peak_packed.restype = c_int
+    L.fw_apsp_auto_report.argtypes = [vp, ctypes.POINTER(c_int)]
+    L.fw_apsp_auto_report.restype = c_int
     L.fw_batch_pack_offsets.argtypes = [vp, i64, vp, ctypes.POINTER(i64)]
     L.fw_batch_pack_offsets.restype = c_int
     L.fw_batch_plan_create.argtypes = [ctypes.POINTER(vp), vp, vp, i64]
@@ -153,6 +160,13 @@ def _stream(stream) -> int | None:
 def apsp_i32(d_D, n: int, tile: int = 0, kappa: int = 0, variant: int = VARIANT_MULTI_LAYER, stream=None) -> None:
     """In-place APSP on the device (enqueued on `stream`; no synchronisation)."""
     _check(lib().fw_apsp_i32(_ptr(d_D), n, tile, kappa, variant, _stream(stream)))
+
+
+def auto_used_packed(stream=None) -> bool:
+    """Whether the last VARIANT_AUTO call on `stream` used the packed path (synchronises)."""
+    v = ctypes.c_int(0)
+    _check(lib().fw_apsp_auto_report(_stream(stream), ctypes.byref(v)))
+    return bool(v.value)
 
 
 def workspace_bytes_i32(n: int, tile: int = 0, kappa: int = 0, variant: int = VARIANT_MULTI_LAYER) -> int:
@@ -202,6 +216,13 @@ def measure_relax_peak(stream=None) -> tuple[float, float]:
     a, b = ctypes.c_double(0), ctypes.c_double(0)
     _check(lib().fw_measure_relax_peak(ctypes.byref(a), ctypes.byref(b), _stream(stream)))
     return a.value, b.value
+
+
+def measure_relax_peak_packed(stream=None) -> float:
+    """Relaxations/s of the register-only packed 16-bit DPX kernel."""
+    a = ctypes.c_double(0)
+    _check(lib().fw_measure_relax_peak_packed(ctypes.byref(a), _stream(stream)))
+    return a.value
 
 
 # ----------------------------------------------------------------- batched APSP

@@ -50,7 +50,8 @@ using DiagClosure = BlockClosure<kTile, 32, 16>;
 template <bool VEC>
 __global__ void __launch_bounds__(kDiagThreads, 1)
     fw_diag_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int64_t p0, int* __restrict__ colT,
-                   int* __restrict__ rowP) {
+                   int* __restrict__ rowP, const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     __shared__ __align__(16) int prow[2 * kTile];
     __shared__ __align__(16) int pcol[2 * kTile];
     constexpr int RR = DiagClosure::RR, RC = DiagClosure::RC;
@@ -108,7 +109,8 @@ __global__ void __launch_bounds__(kDiagThreads, 1)
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_panel_kernel(int* __restrict__ D, int64_t n, int64_t ldp, int pt, int nslab, int* __restrict__ colT,
-                    int* __restrict__ rowP, int one) {
+                    int* __restrict__ rowP, int one, const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int other = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
@@ -154,7 +156,9 @@ __device__ __forceinline__ int tile_of(const TileSet& s, int idx) {
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, TileSet cols, int slab0, int nslab,
-                        const int* __restrict__ colT, const int* __restrict__ rowP, int one) {
+                        const int* __restrict__ colT, const int* __restrict__ rowP, int one,
+                        const unsigned* __restrict__ skip) {
+    if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int64_t r0 = (int64_t)tile_of(rows, blockIdx.y) * kTile, c0 = (int64_t)tile_of(cols, blockIdx.x) * kTile;
@@ -230,6 +234,7 @@ struct Blocked {
     int* colT;  // [rows_per_pass][ldp]
     int* rowP;
     cudaStream_t s;
+    const unsigned* skip;
 
     int64_t p0(int t) const { return (int64_t)t * kTile; }
     int64_t kv(int t) const { return n - p0(t) < kTile ? n - p0(t) : kTile; }
@@ -237,7 +242,8 @@ struct Blocked {
     // Diagonal closure of block t, its panels written to workspace half h.
     int diag(int t, int h) {
         prof_begin(KC_DIAG, s);
-        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, s>>>(D, n, ldp, p0(t), colT + h * kTile * ldp, rowP + h * kTile * ldp);
+        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, s>>>(D, n, ldp, p0(t), colT + h * kTile * ldp, rowP + h * kTile * ldp,
+                                                       skip);
         FW_LAUNCH_CHECK("fw_diag_kernel");
         prof_end(KC_DIAG, s, (double)kv(t) * kv(t) * kv(t));
         return FW_OK;
@@ -247,7 +253,7 @@ struct Blocked {
         const int nslab = (int)((kv(t) + kSlab - 1) / kSlab);
         prof_begin(KC_PANEL, s);
         fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, t, nslab, colT + h * kTile * ldp,
-                                                                         rowP + h * kTile * ldp, 1);
+                                                                         rowP + h * kTile * ldp, 1, skip);
         FW_LAUNCH_CHECK("fw_panel_kernel");
         prof_end(KC_PANEL, s, 2.0 * (double)(n - kv(t)) * kv(t) * kv(t));
         return FW_OK;
@@ -260,7 +266,7 @@ struct Blocked {
         const int nslab = (k_valid + kSlab - 1) / kSlab;
         prof_begin(KC_REMAINDER, s);
         fw_remainder_kernel<VEC><<<dim3(ncols, nrows), kThreads, kSmemBytes, s>>>(D, n, ldp, rows, cols, slab0, nslab,
-                                                                                 colT, rowP, 1);
+                                                                                 colT, rowP, 1, skip);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
         prof_end(KC_REMAINDER, s, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
         return FW_OK;
@@ -309,7 +315,8 @@ struct Blocked {
 };
 
 template <bool VEC>
-int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, int* rowP, cudaStream_t s) {
+int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, int* rowP, cudaStream_t s,
+                       const unsigned* skip) {
     static bool attr_done = false;
     if (!attr_done) {
         FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
@@ -317,7 +324,7 @@ int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, in
             cudaFuncSetAttribute(fw_remainder_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
         attr_done = true;
     }
-    Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s};
+    Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip};
     b.ldp = (int64_t)b.T * kTile;
     for (int t = 0; t < b.T;) {
         if (blocks_per_pass == 2 && t + 1 < b.T) {
@@ -344,13 +351,13 @@ size_t blocked_workspace_bytes(int64_t n, int blocks) {
     return (size_t)2 * blocks * kTile * (size_t)(T * kTile) * sizeof(int);
 }
 
-int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, cudaStream_t s) {
+int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, cudaStream_t s, const unsigned int* skip) {
     const int64_t T = (n + kTile - 1) / kTile;
     int* colT = static_cast<int*>(ws);
     int* rowP = colT + (size_t)blocks * kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    return vec ? blocked_solve_impl<true>(D, n, blocks, colT, rowP, s)
-               : blocked_solve_impl<false>(D, n, blocks, colT, rowP, s);
+    return vec ? blocked_solve_impl<true>(D, n, blocks, colT, rowP, s, skip)
+               : blocked_solve_impl<false>(D, n, blocks, colT, rowP, s, skip);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }

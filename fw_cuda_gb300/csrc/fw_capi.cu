@@ -27,6 +27,9 @@ struct WsEntry {
 };
 std::mutex g_ws_mutex;
 std::map<std::pair<int, cudaStream_t>, WsEntry> g_ws;
+// Device address of the packed path's `done` word of the last FW_VARIANT_AUTO
+// call per (device, stream), for fw_apsp_auto_report.
+std::map<std::pair<int, cudaStream_t>, const unsigned int*> g_auto_done;
 
 // ----------------------------------------------------------------- profiling
 struct ProfState {
@@ -43,8 +46,10 @@ struct ProfState {
 };
 std::mutex g_prof_mutex;
 ProfState g_prof;
-const char* const kClassNames[KC_COUNT] = {"fw_diag", "fw_panel", "fw_remainder", "fw_pivot_step",
-                                           "fw_batched", "fw_forward_f32", "fw_backward_f32"};
+const char* const kClassNames[KC_COUNT] = {"fw_diag",          "fw_panel",        "fw_remainder",
+                                           "fw_pivot_step",    "fw_batched",      "fw_forward_f32",
+                                           "fw_backward_f32",  "fw_p16_diag",     "fw_p16_panel",
+                                           "fw_p16_remainder"};
 
 cudaEvent_t prof_event() {
     if (g_prof.next == g_prof.pool.size()) {
@@ -131,7 +136,8 @@ int check_apsp_args(const int32_t* d_D, int64_t n, int variant) {
     if (n > nmax)
         return set_error(FW_ERR_INVALID_ARGUMENT,
                          "n = " + std::to_string(n) + " exceeds " + std::to_string(nmax) + " for this variant");
-    if (variant != FW_VARIANT_BASELINE && variant != FW_VARIANT_TILING && variant != FW_VARIANT_MULTI_LAYER)
+    if (variant != FW_VARIANT_BASELINE && variant != FW_VARIANT_TILING && variant != FW_VARIANT_MULTI_LAYER &&
+        variant != FW_VARIANT_AUTO)
         return set_error(FW_ERR_INVALID_ARGUMENT, "unknown variant " + std::to_string(variant));
     if ((reinterpret_cast<uintptr_t>(d_D) & 15u) != 0)
         return set_error(FW_ERR_INVALID_ARGUMENT, "d_D must be 16-byte aligned (cudaMalloc memory is)");
@@ -151,7 +157,9 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     (void)kappa;
     if (n < 1) return 0;
     if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
-    return blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
+    const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
+    if (variant == FW_VARIANT_AUTO) return ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
+    return blocked;
 }
 
 int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
@@ -167,7 +175,20 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
         return set_error(FW_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
-    return blocked_solve(d_D, n, blocks_per_pass(variant, kappa), d_workspace, s);
+    const int blocks = blocks_per_pass(variant, kappa);
+    if (variant == FW_VARIANT_AUTO) {
+        const size_t blocked = (blocked_workspace_bytes(n, blocks) + 255) & ~size_t(255);
+        const unsigned int* done = nullptr;
+        if (int rc = p16_solve(d_D, n, static_cast<char*>(d_workspace) + blocked, s, &done)) return rc;
+        {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            std::lock_guard<std::mutex> lk(g_ws_mutex);
+            g_auto_done[{dev, s}] = done;
+        }
+        return blocked_solve(d_D, n, blocks, d_workspace, s, done);
+    }
+    return blocked_solve(d_D, n, blocks, d_workspace, s);
 }
 
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {
@@ -177,6 +198,25 @@ int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_st
     void* ws = workspace_get(s, need);
     if (!ws) return FW_ERR_NO_MEMORY;
     return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, ws, need, stream);
+}
+
+int fw_apsp_auto_report(fw_stream_t stream, int* used_packed) {
+    if (!used_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "used_packed is NULL");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    const unsigned int* done = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_ws_mutex);
+        auto it = g_auto_done.find({dev, s});
+        if (it != g_auto_done.end()) done = it->second;
+    }
+    if (!done) return set_error(FW_ERR_INVALID_ARGUMENT, "no FW_VARIANT_AUTO call on this device and stream");
+    FW_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned int v = 0;
+    FW_CUDA_TRY(cudaMemcpy(&v, done, sizeof(v), cudaMemcpyDeviceToHost));
+    *used_packed = v ? 1 : 0;
+    return FW_OK;
 }
 
 int fw_forward_f32(float* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream) {
@@ -262,6 +302,10 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count) {
 
 int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream) {
     return measure_relax_peak(dpx_only, mixed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int fw_measure_relax_peak_packed(double* packed, fw_stream_t stream) {
+    return measure_relax_peak_packed(packed, reinterpret_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -38,6 +38,9 @@ enum KernelClass {
     KC_BATCHED,
     KC_FWD_F32,
     KC_BWD_F32,
+    KC_P16_DIAG,
+    KC_P16_PANEL,
+    KC_P16_REMAINDER,
     KC_COUNT
 };
 
@@ -57,7 +60,13 @@ int normalise_kappa(int kappa);
 // Blocked-sweep launchers (fw_apsp_i32.cu).
 int blocks_per_pass(int variant, int kappa);
 size_t blocked_workspace_bytes(int64_t n, int blocks);
-int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, cudaStream_t s);
+// `skip`, when not null, is a device flag: nonzero makes every kernel of the
+// sweep return at once (the packed fast path already produced the result).
+int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, cudaStream_t s, const unsigned int* skip = nullptr);
+
+// Exact packed 16-bit fast path (fw_packed16.cu).
+size_t p16_workspace_bytes(int64_t n);
+int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag);
 size_t pivot_workspace_bytes(int64_t n);
 int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 
@@ -68,5 +77,6 @@ int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t ba
 
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);
+int measure_relax_peak_packed(double* packed, cudaStream_t s);
 
 }  // namespace fw

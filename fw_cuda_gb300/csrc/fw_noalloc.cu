@@ -68,6 +68,8 @@ extern "C" int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa,
     // The two-block schedule of kappa > 4 needs twice the panel workspace;
     // kappa only selects the schedule, not the result, so cap it here.
     if (kappa > 4) kappa = 4;
+    // The packed fast path needs an n x n 16-bit copy; here the int32 sweep runs.
+    if (variant == FW_VARIANT_AUTO) variant = FW_VARIANT_MULTI_LAYER;
     if (n > kNoAllocMaxN)
         return fw::set_error(FW_ERR_INVALID_ARGUMENT,
                              "fw_apsp_i32_noalloc: n = " + std::to_string(n) +

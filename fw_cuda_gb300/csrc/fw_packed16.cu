@@ -1,0 +1,424 @@
+// Exact packed 16-bit fast path for the int32 sweep (FW_VARIANT_AUTO).
+//
+// Every relaxation of the int32 sweep runs here as one half of a packed
+// `__viaddmin_u16x2`, two relaxations per DPX instruction, on a 16-bit copy of
+// the matrix, and the result is written back to the int32 matrix only when it
+// is provably identical to what the int32 sweep (and so the reference's
+// baseline_cpu, src/fw_baseline_cpu.cpp:6-15) returns; otherwise the int32
+// blocked sweep runs instead. The decision is taken on the device, so the
+// call stays asynchronous.
+//
+// Why it is exact. Let CAP = 32767. The input qualifies when every entry is
+// either INF or an integer in [0, CAP). Entries are encoded as themselves,
+// INF as CAP. Sums of two encoded values stay below 65535, so the packed
+// add never wraps, and min(c, a + b) never exceeds CAP: the sweep computes the
+// min-plus closure over [0, CAP] with every value = min(CAP, d), d the true
+// shortest-path length over the real edges (weights are non-negative, so a
+// path shorter than CAP has only prefixes shorter than CAP, all computed
+// exactly). The int32 sweep returns d for reachable pairs and INF for the
+// others. So entries below CAP are exact, and an entry equal to CAP is INF
+// unless some finite d >= CAP exists. If one did, its shortest path would
+// pass a vertex u whose prefix length lies in [CAP - w_max, CAP) (prefixes
+// grow by at most the largest edge weight w_max), and d(i, u) is that prefix
+// length. Hence: if the largest result below CAP is below CAP - w_max, every
+// CAP entry is INF and decoding is exact; if not, the int32 sweep runs.
+//
+// Layout: D16 is the matrix as uint16, leading dimension ld16 = n rounded up
+// to 256, padded with CAP (padded vertices have no edges). Tiles are
+// 256 x 256 values on 512-thread CTAs; each thread holds 8 rows x 8 words
+// (16 columns) in registers. The pivot block is 256 wide. The column panel is
+// kept transposed in a workspace as 32-bit words with the 16-bit value in both
+// halves (colD[k][i] = v | v << 16, the A operand of the packed add), the row
+// panel as plain packed rows (rowP[k][*], the B operand).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "fw_common.cuh"
+#include "fw_internal.h"
+
+namespace fw {
+namespace {
+
+constexpr uint32_t kCap = 0x7FFF;
+constexpr int kPT = 256;           // tile / pivot block (values)
+constexpr int kPW = kPT / 2;       // tile width in 32-bit words
+constexpr int kPThreads = 512;     // 32 row groups x 16 word groups
+constexpr int kPStages = 3;
+constexpr int kPSlabA = kSlab * kPT;   // words: 32 pivots x 256 rows (duplicated values)
+constexpr int kPSlabB = kSlab * kPW;   // words: 32 pivots x 128 words
+constexpr int kPStageWords = kPSlabA + kPSlabB;
+constexpr int kPSmemBytes = kPStages * kPStageWords * 4;  // 144 KB
+
+struct P16Status {
+    unsigned int ineligible;  // nonzero: some entry is neither INF nor in [0, CAP)
+    unsigned int wmax;        // largest finite input entry
+    unsigned int rmax;        // largest result entry below CAP
+    unsigned int done;        // 1: D holds the decoded packed result
+};
+
+__device__ __forceinline__ uint32_t dup16(uint32_t v) { return v | (v << 16); }
+
+// Rows and words of a thread (tx = t % 16, ty = t / 16) in a 256 x 256 tile.
+__device__ __forceinline__ int prow_of(int ty, int r) { return (r < 4) ? ty * 4 + r : 128 + ty * 4 + (r - 4); }
+__device__ __forceinline__ int pword_of(int tx, int w) { return (w < 4) ? tx * 4 + w : 64 + tx * 4 + (w - 4); }
+
+// ------------------------------------------------------------ encode / decode
+__global__ void fw_p16_encode_kernel(const int* __restrict__ D, int64_t n, uint16_t* __restrict__ D16, int64_t ld16,
+                                     P16Status* st) {
+    unsigned bad = 0, wmax = 0;
+    const int64_t total = ld16 * ld16;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = q / ld16, j = q % ld16;
+        uint32_t e = kCap;
+        if (i < n && j < n) {
+            const int v = D[i * n + j];
+            if (v == kInf) {
+                e = kCap;
+            } else if (v >= 0 && (uint32_t)v < kCap) {
+                e = (uint32_t)v;
+                wmax = max(wmax, (unsigned)v);
+            } else {
+                bad = 1;
+            }
+        }
+        D16[q] = (uint16_t)e;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+        wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicOr(&st->ineligible, 1u);
+        if (wmax) atomicMax(&st->wmax, wmax);
+    }
+}
+
+__global__ void fw_p16_rmax_kernel(const uint16_t* __restrict__ D16, int64_t n, int64_t ld16, P16Status* st) {
+    if (st->ineligible) return;
+    unsigned m = 0;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = D16[(q / n) * ld16 + q % n];
+        if (v < kCap) m = max(m, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&st->rmax, m);
+}
+
+__global__ void fw_p16_decode_kernel(const uint16_t* __restrict__ D16, int* __restrict__ D, int64_t n, int64_t ld16,
+                                     P16Status* st) {
+    if (st->ineligible || st->rmax + st->wmax >= kCap) return;  // the int32 sweep runs instead
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = D16[(q / n) * ld16 + q % n];
+        D[q] = (v == kCap) ? kInf : (int)v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+}
+
+// ------------------------------------------------------------ tile helpers
+__device__ __forceinline__ const uint32_t* words(const uint16_t* p) { return reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void p_load_tile(uint32_t (&c)[8][8], const uint16_t* D16, int64_t ldw, int64_t r0,
+                                            int64_t w0, int tx, int ty) {
+    const uint32_t* Dw = words(D16);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const uint32_t* row = Dw + (r0 + prow_of(ty, r)) * ldw + w0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint4 t = *reinterpret_cast<const uint4*>(row + h * 64 + tx * 4);
+            c[r][h * 4 + 0] = t.x; c[r][h * 4 + 1] = t.y; c[r][h * 4 + 2] = t.z; c[r][h * 4 + 3] = t.w;
+        }
+    }
+}
+
+__device__ __forceinline__ void p_store_tile(const uint32_t (&c)[8][8], uint16_t* D16, int64_t ldw, int64_t r0,
+                                             int64_t w0, int tx, int ty) {
+    uint32_t* Dw = reinterpret_cast<uint32_t*>(D16);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        uint32_t* row = Dw + (r0 + prow_of(ty, r)) * ldw + w0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            *reinterpret_cast<uint4*>(row + h * 64 + tx * 4) =
+                make_uint4(c[r][h * 4 + 0], c[r][h * 4 + 1], c[r][h * 4 + 2], c[r][h * 4 + 3]);
+    }
+}
+
+// Transposed, duplicated store of the tile: colD[k][r0 + i] = dup(tile[i][k]).
+__device__ __forceinline__ void p_store_coldup(const uint32_t (&c)[8][8], uint32_t* colD, int64_t ldc, int64_t r0,
+                                               int tx, int ty) {
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        const int k0 = 2 * pword_of(tx, w);
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            uint32_t v[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[r] = dup16(half ? (c[r][w] >> 16) : (c[r][w] & 0xFFFFu));
+            uint32_t* dst = colD + (int64_t)(k0 + half) * ldc + r0 + ty * 4;
+            *reinterpret_cast<uint4*>(dst) = make_uint4(v[0], v[1], v[2], v[3]);
+            *reinterpret_cast<uint4*>(dst + 128) = make_uint4(v[4], v[5], v[6], v[7]);
+        }
+    }
+}
+
+// Slab of a k-major word buffer: rows [k0, k0 + 32), `width` words from c0.
+template <int WIDTH>
+__device__ __forceinline__ void p_load_kmajor(uint32_t* dst, const uint32_t* buf, int64_t ld, int k0, int64_t c0,
+                                              int tid) {
+    constexpr int CH = WIDTH / 4;  // 16-byte chunks per row
+    for (int q = tid; q < kSlab * CH; q += kPThreads) {
+        const int row = q / CH, ch = q % CH;
+        cp_async16(dst + row * WIDTH + ch * 4, buf + (int64_t)(k0 + row) * ld + c0 + ch * 4);
+    }
+}
+
+// Transposed, duplicated slab of D16: dst[kk][i] = dup(D16[r0 + i][p0 + k0 + kk]).
+__device__ __forceinline__ void p_load_transposed_dup(uint32_t* dst, const uint16_t* D16, int64_t ld16, int64_t r0,
+                                                      int64_t kcol0, int tid) {
+    for (int q = tid; q < kPT * (kSlab / 2); q += kPThreads) {
+        const int i = q / (kSlab / 2), wp = q % (kSlab / 2);
+        const uint32_t w = words(D16)[((r0 + i) * ld16 + kcol0) / 2 + wp];
+        dst[(2 * wp) * kPT + i] = dup16(w & 0xFFFFu);
+        dst[(2 * wp + 1) * kPT + i] = dup16(w >> 16);
+    }
+}
+
+__device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t* As, const uint32_t* Bs, int tx,
+                                             int ty) {
+#pragma unroll 1
+    for (int kk = 0; kk < kSlab; ++kk) {
+        const uint4 a0 = *reinterpret_cast<const uint4*>(As + kk * kPT + ty * 4);
+        const uint4 a1 = *reinterpret_cast<const uint4*>(As + kk * kPT + 128 + ty * 4);
+        const uint4 b0 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + tx * 4);
+        const uint4 b1 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + 64 + tx * 4);
+        const uint32_t a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const uint32_t b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int w = 0; w < 8; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
+    }
+}
+
+template <class LA, class LB>
+__device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint32_t* smem, LA la, LB lb, int tx,
+                                           int ty) {
+#pragma unroll
+    for (int s = 0; s < kPStages - 1; ++s) {
+        if (s < nslab) {
+            la(smem + s * kPStageWords, s);
+            lb(smem + s * kPStageWords + kPSlabA, s);
+        }
+        cp_async_commit();
+    }
+    for (int kb = 0; kb < nslab; ++kb) {
+        cp_async_wait<kPStages - 2>();
+        __syncthreads();
+        const int nxt = kb + kPStages - 1;
+        if (nxt < nslab) {
+            uint32_t* st = smem + (nxt % kPStages) * kPStageWords;
+            la(st, nxt);
+            lb(st + kPSlabA, nxt);
+        }
+        cp_async_commit();
+        const uint32_t* st = smem + (kb % kPStages) * kPStageWords;
+        p_relax_slab(c, st, st + kPSlabA, tx, ty);
+    }
+}
+
+// ------------------------------------------------------------ kernels
+// Closure of the 256 x 256 pivot block, one CTA; writes D16, colD (transposed,
+// duplicated) and rowP (packed rows) for the block.
+__global__ void __launch_bounds__(kPThreads, 1)
+    fw_p16_diag_kernel(uint16_t* __restrict__ D16, int64_t ld16, int64_t p0, uint32_t* __restrict__ colD,
+                       uint32_t* __restrict__ rowP, const P16Status* st) {
+    if (st->ineligible) return;
+    __shared__ __align__(16) uint32_t prw[2][kPW];  // pivot row, packed
+    __shared__ __align__(16) uint32_t pcl[2][kPT];  // pivot column, duplicated
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const int64_t ldw = ld16 / 2;
+    uint32_t c[8][8];
+    p_load_tile(c, D16, ldw, p0, p0 / 2, tx, ty);
+    // pivot 0: row 0 is rows r = 0 of ty = 0; column 0 is the low half of word 0 (tx = 0, w = 0)
+    if (ty == 0) {
+#pragma unroll
+        for (int w = 0; w < 8; ++w) prw[0][pword_of(tx, w)] = c[0][w];
+    }
+    if (tx == 0) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) pcl[0][prow_of(ty, r)] = dup16(c[r][0] & 0xFFFFu);
+    }
+    __syncthreads();
+    for (int kb = 0; kb < kPT; kb += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = kb + u, buf = u & 1;
+            uint32_t a[8], b[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) a[r] = pcl[buf][prow_of(ty, r)];
+#pragma unroll
+            for (int w = 0; w < 8; ++w) b[w] = prw[buf][pword_of(tx, w)];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int w = 0; w < 8; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
+            const int k1 = k + 1;
+            if (k1 < kPT) {
+                // row k1: ty = (k1 % 128) / 4, r = (k1 >= 128 ? 4 : 0) + k1 % 4
+                const int rsel = (u + 1) & 3;
+                const bool upper = k1 >= 128;
+                if (ty == ((k1 & 127) >> 2)) {
+#pragma unroll
+                    for (int w = 0; w < 8; ++w) prw[buf ^ 1][pword_of(tx, w)] = upper ? c[4 + rsel][w] : c[rsel][w];
+                }
+                // column k1: word k1 / 2, half k1 % 2; owner tx = (word % 64) / 4, w = (word >= 64 ? 4 : 0) + word % 4
+                const int word = k1 >> 1, half = k1 & 1;
+                if (tx == ((word & 63) >> 2)) {
+                    const int wsel = (word >= 64 ? 4 : 0) + (word & 3);
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        uint32_t x = 0;
+#pragma unroll
+                        for (int w = 0; w < 8; ++w)
+                            if (w == wsel) x = c[r][w];
+                        pcl[buf ^ 1][prow_of(ty, r)] = dup16(half ? (x >> 16) : (x & 0xFFFFu));
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    p_store_tile(c, D16, ldw, p0, p0 / 2, tx, ty);
+    p_store_coldup(c, colD, ld16, p0, tx, ty);
+    // rowP rows are the pivot rows k = p0.. as packed words, ld = ld16 / 2
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        uint32_t* row = rowP + (int64_t)prow_of(ty, r) * ldw + p0 / 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            *reinterpret_cast<uint4*>(row + h * 64 + tx * 4) =
+                make_uint4(c[r][h * 4 + 0], c[r][h * 4 + 1], c[r][h * 4 + 2], c[r][h * 4 + 3]);
+    }
+}
+
+// blockIdx.y == 0: row panel tile (P, J); == 1: column panel tile (I, P).
+__global__ void __launch_bounds__(kPThreads, 1)
+    fw_p16_panel_kernel(uint16_t* __restrict__ D16, int64_t ld16, int pt, uint32_t* __restrict__ colD,
+                        uint32_t* __restrict__ rowP, const P16Status* st) {
+    if (st->ineligible) return;
+    extern __shared__ __align__(128) uint32_t psm[];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const int other = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
+    const int64_t p0 = (int64_t)pt * kPT, q0 = (int64_t)other * kPT, ldw = ld16 / 2;
+    uint32_t c[8][8];
+    if (blockIdx.y == 0) {
+        p_load_tile(c, D16, ldw, p0, q0 / 2, tx, ty);
+        p_mainloop(
+            c, kPT / kSlab, psm, [&](uint32_t* dst, int s) { p_load_kmajor<kPT>(dst, colD, ld16, s * kSlab, p0, tid); },
+            [&](uint32_t* dst, int s) {
+                p_load_kmajor<kPW>(dst, words(D16), ldw, (int)(p0 + s * kSlab), q0 / 2, tid);
+            },
+            tx, ty);
+        p_store_tile(c, D16, ldw, p0, q0 / 2, tx, ty);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            uint32_t* row = rowP + (int64_t)prow_of(ty, r) * ldw + q0 / 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                *reinterpret_cast<uint4*>(row + h * 64 + tx * 4) =
+                    make_uint4(c[r][h * 4 + 0], c[r][h * 4 + 1], c[r][h * 4 + 2], c[r][h * 4 + 3]);
+        }
+    } else {
+        p_load_tile(c, D16, ldw, q0, p0 / 2, tx, ty);
+        p_mainloop(
+            c, kPT / kSlab, psm,
+            [&](uint32_t* dst, int s) { p_load_transposed_dup(dst, D16, ld16, q0, p0 + s * kSlab, tid); },
+            [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, p0 / 2, tid); }, tx, ty);
+        p_store_tile(c, D16, ldw, q0, p0 / 2, tx, ty);
+        p_store_coldup(c, colD, ld16, q0, tx, ty);
+    }
+}
+
+// Remainder tile (I, J), both different from the pivot block.
+__global__ void __launch_bounds__(kPThreads, 1)
+    fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, int pt, const uint32_t* __restrict__ colD,
+                            const uint32_t* __restrict__ rowP, const P16Status* st) {
+    if (st->ineligible) return;
+    extern __shared__ __align__(128) uint32_t psm[];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
+    const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
+    const int64_t r0 = (int64_t)ti * kPT, w0 = (int64_t)tj * kPW, ldw = ld16 / 2;
+    uint32_t c[8][8];
+    p_load_tile(c, D16, ldw, r0, w0, tx, ty);
+    p_mainloop(
+        c, kPT / kSlab, psm, [&](uint32_t* dst, int s) { p_load_kmajor<kPT>(dst, colD, ld16, s * kSlab, r0, tid); },
+        [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, w0, tid); }, tx, ty);
+    p_store_tile(c, D16, ldw, r0, w0, tx, ty);
+}
+
+}  // namespace
+
+int64_t p16_ld(int64_t n) { return (n + kPT - 1) / kPT * kPT; }
+
+size_t p16_workspace_bytes(int64_t n) {
+    const int64_t ld = p16_ld(n);
+    return 256                                   // status
+           + (size_t)ld * ld * 2                 // D16
+           + (size_t)kPT * ld * 4                // colD (duplicated words)
+           + (size_t)kPT * (ld / 2) * 4;         // rowP (packed words)
+}
+
+// Enqueues encode, the packed sweep and the guarded decode; *status_out
+// receives the device address of the status word whose `done` field tells
+// the int32 kernels to skip.
+int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
+    static bool attr_done = false;
+    if (!attr_done) {
+        FW_CUDA_TRY(cudaFuncSetAttribute(fw_p16_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+        FW_CUDA_TRY(
+            cudaFuncSetAttribute(fw_p16_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+        attr_done = true;
+    }
+    const int64_t ld = p16_ld(n);
+    const int T = (int)(ld / kPT);
+    char* base = static_cast<char*>(ws);
+    P16Status* st = reinterpret_cast<P16Status*>(base);
+    uint16_t* D16 = reinterpret_cast<uint16_t*>(base + 256);
+    uint32_t* colD = reinterpret_cast<uint32_t*>(base + 256 + (size_t)ld * ld * 2);
+    uint32_t* rowP = colD + (size_t)kPT * ld;
+    FW_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(P16Status), s));
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)(sms > 0 ? sms * 8 : 1024);
+    fw_p16_encode_kernel<<<grid, 256, 0, s>>>(D, n, D16, ld, st);
+    FW_LAUNCH_CHECK("fw_p16_encode_kernel");
+    for (int pt = 0; pt < T; ++pt) {
+        const double kv = (double)((n - (int64_t)pt * kPT) < kPT ? n - (int64_t)pt * kPT : kPT);
+        prof_begin(KC_P16_DIAG, s);
+        fw_p16_diag_kernel<<<1, kPThreads, 0, s>>>(D16, ld, (int64_t)pt * kPT, colD, rowP, st);
+        FW_LAUNCH_CHECK("fw_p16_diag_kernel");
+        prof_end(KC_P16_DIAG, s, kv * kv * kv);
+        if (T > 1) {
+            prof_begin(KC_P16_PANEL, s);
+            fw_p16_panel_kernel<<<dim3(T - 1, 2), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st);
+            FW_LAUNCH_CHECK("fw_p16_panel_kernel");
+            prof_end(KC_P16_PANEL, s, 2.0 * ((double)n - kv) * kv * kv);
+            prof_begin(KC_P16_REMAINDER, s);
+            fw_p16_remainder_kernel<<<dim3(T - 1, T - 1), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st);
+            FW_LAUNCH_CHECK("fw_p16_remainder_kernel");
+            prof_end(KC_P16_REMAINDER, s, ((double)n - kv) * ((double)n - kv) * kv);
+        }
+    }
+    fw_p16_rmax_kernel<<<grid, 256, 0, s>>>(D16, n, ld, st);
+    FW_LAUNCH_CHECK("fw_p16_rmax_kernel");
+    fw_p16_decode_kernel<<<grid, 256, 0, s>>>(D16, D, n, ld, st);
+    FW_LAUNCH_CHECK("fw_p16_decode_kernel");
+    *done_flag = &st->done;
+    return FW_OK;
+}
+
+}  // namespace fw

@@ -48,6 +48,25 @@ __global__ void __launch_bounds__(256) fw_peak_kernel(const int* __restrict__ in
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Packed 16-bit DPX add-min: two relaxations per instruction, 16 accumulators
+// of two lanes each, operands from other accumulators.
+__global__ void __launch_bounds__(256) fw_peak_packed_kernel(const unsigned* __restrict__ in, unsigned* __restrict__ out,
+                                                             int iters) {
+    unsigned acc[16], a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a[r] = in[(threadIdx.x + r) & 255] & 0x3FFF3FFFu;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = in[256 + ((threadIdx.x + q) & 255)] & 0x3FFF3FFFu;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] = __viaddmin_u16x2(a[q & 3], acc[(q + 1) & 15], acc[q]);
+    }
+    unsigned s = 0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) s ^= acc[q];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 template <int MIXA>
 int time_peak(int blocks, const int* in, int* out, cudaStream_t s, double* rate) {
     cudaEvent_t e0, e1;
@@ -76,6 +95,43 @@ int time_peak(int blocks, const int* in, int* out, cudaStream_t s, double* rate)
 }
 
 }  // namespace
+
+int measure_relax_peak_packed(double* packed, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8;
+    unsigned *in = nullptr, *out = nullptr;
+    FW_CUDA_TRY(cudaMallocAsync(&in, 512 * sizeof(unsigned), s));
+    FW_CUDA_TRY(cudaMallocAsync(&out, (size_t)blocks * 256 * sizeof(unsigned), s));
+    FW_CUDA_TRY(cudaMemsetAsync(in, 0, 512 * sizeof(unsigned), s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int rc = FW_OK;
+    for (int rep = 0; rep < 5 && rc == FW_OK; ++rep) {
+        cudaEventRecord(e0, s);
+        fw_peak_packed_kernel<<<blocks, 256, 0, s>>>(in, out, kPeakIters);
+        cudaEventRecord(e1, s);
+        const cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "fw_peak_packed_kernel");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(in, s);
+    cudaFreeAsync(out, s);
+    if (rc) return rc;
+    // 16 accumulators x 2 lanes per iteration.
+    if (packed) *packed = (double)blocks * 256.0 * kPeakIters * 32.0 / (best * 1e-3);
+    return FW_OK;
+}
 
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s) {
     int dev = 0, sms = 0;

@@ -46,7 +46,8 @@ typedef enum fw_status {
 typedef enum fw_variant {
     FW_VARIANT_BASELINE = 0,    /* "baseline_gpu": one relaxation sweep per pivot */
     FW_VARIANT_TILING = 1,      /* "tiling_gpu": blocked sweep, 128-wide pivot blocks */
-    FW_VARIANT_MULTI_LAYER = 2  /* "multi_layer_tiling_gpu": kappa pivot layers per pass */
+    FW_VARIANT_MULTI_LAYER = 2, /* "multi_layer_tiling_gpu": kappa pivot layers per pass */
+    FW_VARIANT_AUTO = 3         /* exact packed 16-bit sweep when provably identical, else MULTI_LAYER */
 } fw_variant;
 
 /* ---------------------------------------------------------------- plain APSP */
@@ -61,6 +62,12 @@ typedef enum fw_variant {
  * src/fw_multi_layer_tiling_gpu.cu:511-513). Uses a per-(device, stream)
  * workspace that the library allocates on first use and keeps. */
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
+
+/* After a FW_VARIANT_AUTO call on `stream`: synchronises the stream and sets
+ * *used_packed to 1 if the exact packed 16-bit sweep produced the result, 0 if
+ * the int32 sweep ran (input outside [0, 32767) u {INF}, or distances too
+ * close to the 16-bit cap to prove the packed result exact). */
+int fw_apsp_auto_report(fw_stream_t stream, int* used_packed);
 
 /* Bytes of device workspace fw_apsp_i32_ws needs for these arguments. */
 size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant);
@@ -169,6 +176,10 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count);
  * relaxation is one DPX add-min instruction (dpx_only), and the best rate of
  * the instruction mix the blocked kernels use (mixed). */
 int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream);
+
+/* The same for the packed 16-bit DPX add-min of FW_VARIANT_AUTO's fast path
+ * (two relaxations per instruction). */
+int fw_measure_relax_peak_packed(double* packed, fw_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ from conftest import GOLDEN, load_json, sha
 pytestmark = pytest.mark.gpu
 
 INF = 1_000_000_000
-VARIANTS = {"baseline_gpu": 0, "tiling_gpu": 1, "multi_layer_tiling_gpu": 2}
+VARIANTS = {"baseline_gpu": 0, "tiling_gpu": 1, "multi_layer_tiling_gpu": 2, "auto": 3}
 
 
 def solve(fw, torch, W: np.ndarray, variant: int, kappa: int = 0, tile: int = 0) -> np.ndarray:
@@ -85,7 +85,7 @@ def test_ragged_sizes(fw, cuda, oracle, n):
     for name, v in VARIANTS.items():
         if name == "baseline_gpu" and n > 700:
             continue
-        for kappa in ((1, 4, 8) if v == 2 else (0,)):
+        for kappa in ((1, 4, 8) if v == 2 else (4, 8) if v == 3 else (0,)):
             assert np.array_equal(solve(fw, cuda, W, v, kappa=kappa), ref), (name, n, kappa)
 
 
@@ -109,7 +109,7 @@ def test_negative_cycle_detected_and_deterministic(fw, cuda, oracle, n):
         W[a, b] = -40
     ref = oracle.fw_i32(W)
     assert oracle.has_negative_cycle(ref)
-    for v in (1, 2):
+    for v in (0, 1, 2, 3):
         out1 = solve(fw, cuda, W, v)
         out2 = solve(fw, cuda, W, v)
         assert np.any(np.diag(out1) < 0)
@@ -137,6 +137,7 @@ def test_config_c2_kappa_sweep(fw, cuda, oracle):
     for kappa in (1, 2, 4, 6, 8):
         outs.add(sha(solve(fw, cuda, a, 2, kappa=kappa)))
     outs.add(sha(solve(fw, cuda, a, 1)))
+    outs.add(sha(solve(fw, cuda, a, 3, kappa=8)))
     assert len(outs) == 1
     if want is not None:
         assert outs == {want}
@@ -174,7 +175,7 @@ def test_registry_functions_synchronise(fw, cuda, oracle):
     n = 200
     W = oracle.generate_graph(n, 0.4, 1, 0, 25000)
     ref = oracle.fw_i32(W)
-    for name in ("baseline_gpu", "tiling_gpu", "multi_layer_tiling_gpu"):
+    for name in fw.GPU_ALGORITHMS:
         d = cuda.from_numpy(W).cuda()
         fw.get_gpu_algorithm_func(name)(d, n, 32, 4)
         assert np.array_equal(d.cpu().numpy(), ref), name
