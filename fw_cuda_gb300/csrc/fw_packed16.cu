@@ -185,26 +185,52 @@ __device__ __forceinline__ void p_load_transposed_dup(uint32_t* dst, const uint1
     }
 }
 
+// Number of the 8 word columns that fold a pivot pair with two packed DPX
+// add-mins; the others add with two 32-bit multiply-adds (exact as packed
+// adds: each half stays below 65535, so no carry crosses the halves) on the
+// FMA pipe and take one packed three-way DPX min.
+constexpr int kP16MixA = 8;
+
+template <int MIXW>
 __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t* As, const uint32_t* Bs, int tx,
-                                             int ty) {
+                                             int ty, int one) {
 #pragma unroll 1
-    for (int kk = 0; kk < kSlab; ++kk) {
-        const uint4 a0 = *reinterpret_cast<const uint4*>(As + kk * kPT + ty * 4);
-        const uint4 a1 = *reinterpret_cast<const uint4*>(As + kk * kPT + 128 + ty * 4);
-        const uint4 b0 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + tx * 4);
-        const uint4 b1 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + 64 + tx * 4);
-        const uint32_t a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const uint32_t b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+    for (int kk = 0; kk < kSlab; kk += 2) {
+        uint32_t a0[8], b0[8], a1[8], b1[8];
+        {
+            const uint4 x0 = *reinterpret_cast<const uint4*>(As + kk * kPT + ty * 4);
+            const uint4 x1 = *reinterpret_cast<const uint4*>(As + kk * kPT + 128 + ty * 4);
+            const uint4 y0 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + tx * 4);
+            const uint4 y1 = *reinterpret_cast<const uint4*>(Bs + kk * kPW + 64 + tx * 4);
+            a0[0] = x0.x; a0[1] = x0.y; a0[2] = x0.z; a0[3] = x0.w; a0[4] = x1.x; a0[5] = x1.y; a0[6] = x1.z; a0[7] = x1.w;
+            b0[0] = y0.x; b0[1] = y0.y; b0[2] = y0.z; b0[3] = y0.w; b0[4] = y1.x; b0[5] = y1.y; b0[6] = y1.z; b0[7] = y1.w;
+        }
+        {
+            const uint4 x0 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kPT + ty * 4);
+            const uint4 x1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kPT + 128 + ty * 4);
+            const uint4 y0 = *reinterpret_cast<const uint4*>(Bs + (kk + 1) * kPW + tx * 4);
+            const uint4 y1 = *reinterpret_cast<const uint4*>(Bs + (kk + 1) * kPW + 64 + tx * 4);
+            a1[0] = x0.x; a1[1] = x0.y; a1[2] = x0.z; a1[3] = x0.w; a1[4] = x1.x; a1[5] = x1.y; a1[6] = x1.z; a1[7] = x1.w;
+            b1[0] = y0.x; b1[1] = y0.y; b1[2] = y0.z; b1[3] = y0.w; b1[4] = y1.x; b1[5] = y1.y; b1[6] = y1.z; b1[7] = y1.w;
+        }
 #pragma unroll
         for (int r = 0; r < 8; ++r)
 #pragma unroll
-            for (int w = 0; w < 8; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
+            for (int w = 0; w < 8; ++w) {
+                if (w < MIXW) {
+                    c[r][w] = __viaddmin_u16x2(a1[r], b1[w], __viaddmin_u16x2(a0[r], b0[w], c[r][w]));
+                } else {
+                    const uint32_t s0 = (uint32_t)add_on_fma((int)a0[r], (int)b0[w], one);
+                    const uint32_t s1 = (uint32_t)add_on_fma((int)a1[r], (int)b1[w], one);
+                    c[r][w] = __vimin3_u16x2(c[r][w], s0, s1);
+                }
+            }
     }
 }
 
-template <class LA, class LB>
+template <int MIXW = kP16MixA, class LA, class LB>
 __device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint32_t* smem, LA la, LB lb, int tx,
-                                           int ty) {
+                                           int ty, int one) {
 #pragma unroll
     for (int s = 0; s < kPStages - 1; ++s) {
         if (s < nslab) {
@@ -224,7 +250,7 @@ __device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint3
         }
         cp_async_commit();
         const uint32_t* st = smem + (kb % kPStages) * kPStageWords;
-        p_relax_slab(c, st, st + kPSlabA, tx, ty);
+        p_relax_slab<MIXW>(c, st, st + kPSlabA, tx, ty, one);
     }
 }
 
@@ -306,7 +332,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
 // blockIdx.y == 0: row panel tile (P, J); == 1: column panel tile (I, P).
 __global__ void __launch_bounds__(kPThreads, 1)
     fw_p16_panel_kernel(uint16_t* __restrict__ D16, int64_t ld16, int pt, uint32_t* __restrict__ colD,
-                        uint32_t* __restrict__ rowP, const P16Status* st) {
+                        uint32_t* __restrict__ rowP, const P16Status* st, int one) {
     if (st->ineligible) return;
     extern __shared__ __align__(128) uint32_t psm[];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
@@ -320,7 +346,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
             [&](uint32_t* dst, int s) {
                 p_load_kmajor<kPW>(dst, words(D16), ldw, (int)(p0 + s * kSlab), q0 / 2, tid);
             },
-            tx, ty);
+            tx, ty, one);
         p_store_tile(c, D16, ldw, p0, q0 / 2, tx, ty);
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
@@ -335,7 +361,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
         p_mainloop(
             c, kPT / kSlab, psm,
             [&](uint32_t* dst, int s) { p_load_transposed_dup(dst, D16, ld16, q0, p0 + s * kSlab, tid); },
-            [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, p0 / 2, tid); }, tx, ty);
+            [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, p0 / 2, tid); }, tx, ty, one);
         p_store_tile(c, D16, ldw, q0, p0 / 2, tx, ty);
         p_store_coldup(c, colD, ld16, q0, tx, ty);
     }
@@ -344,7 +370,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
 // Remainder tile (I, J), both different from the pivot block.
 __global__ void __launch_bounds__(kPThreads, 1)
     fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, int pt, const uint32_t* __restrict__ colD,
-                            const uint32_t* __restrict__ rowP, const P16Status* st) {
+                            const uint32_t* __restrict__ rowP, const P16Status* st, int one) {
     if (st->ineligible) return;
     extern __shared__ __align__(128) uint32_t psm[];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
@@ -355,7 +381,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
     p_load_tile(c, D16, ldw, r0, w0, tx, ty);
     p_mainloop(
         c, kPT / kSlab, psm, [&](uint32_t* dst, int s) { p_load_kmajor<kPT>(dst, colD, ld16, s * kSlab, r0, tid); },
-        [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, w0, tid); }, tx, ty);
+        [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, w0, tid); }, tx, ty, one);
     p_store_tile(c, D16, ldw, r0, w0, tx, ty);
 }
 
@@ -404,11 +430,12 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
         prof_end(KC_P16_DIAG, s, kv * kv * kv);
         if (T > 1) {
             prof_begin(KC_P16_PANEL, s);
-            fw_p16_panel_kernel<<<dim3(T - 1, 2), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st);
+            fw_p16_panel_kernel<<<dim3(T - 1, 2), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st, 1);
             FW_LAUNCH_CHECK("fw_p16_panel_kernel");
             prof_end(KC_P16_PANEL, s, 2.0 * ((double)n - kv) * kv * kv);
             prof_begin(KC_P16_REMAINDER, s);
-            fw_p16_remainder_kernel<<<dim3(T - 1, T - 1), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st);
+            fw_p16_remainder_kernel<<<dim3(T - 1, T - 1), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st,
+                                                                                        1);
             FW_LAUNCH_CHECK("fw_p16_remainder_kernel");
             prof_end(KC_P16_REMAINDER, s, ((double)n - kv) * ((double)n - kv) * kv);
         }
