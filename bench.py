@@ -107,7 +107,7 @@ class ClockSampler:
                 self.thread.join(timeout=2)
 
     def summary(self) -> dict:
-        sm, smax, reasons = [], None, set()
+        sm, smax, reasons, power = [], None, set(), []
         names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.lines:
             parts = [p.strip() for p in line.split(",")]
@@ -116,12 +116,14 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 smax = float(parts[2])
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, val in zip(names[1:], parts[5:9]):
                 if val.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "sm_mhz_min": min(sm) if sm else None, "power_w_median": statistics.median(power) if power else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -229,15 +231,16 @@ def run_ours(args) -> None:
         t1 = torch.cuda.Event(enable_timing=True)
         t2 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        t1.record(stream)
-        for _ in range(args.steps):
-            e2e_step()
-        t2.record(stream)
-        torch.cuda.synchronize()
+        with ClockSampler(local) as e2e_clocks:
+            t1.record(stream)
+            for _ in range(args.steps):
+                e2e_step()
+            t2.record(stream)
+            torch.cuda.synchronize()
         e2e_s = max_over_ranks(t1.elapsed_time(t2) / 1e3, world)
         e2e = {"value": aggregate(world, args.steps, relax, e2e_s), "unit": UNIT,
                "h2d_bytes_per_step": 4 * n * n, "d2h_bytes_per_step": 4 * n * n,
-               "ms_per_step": 1e3 * e2e_s / args.steps}
+               "ms_per_step": 1e3 * e2e_s / args.steps, "clocks": e2e_clocks.summary()}
         # Cheap sanity check of the last result: the diagonal is 0 and no entry
         # exceeds its input edge weight.
         assert torch.all(torch.diagonal(work) == 0).item()
