@@ -49,6 +49,10 @@ EXPORTED_SYMBOLS = (
     "fw_measure_relax_peak",
     "fw_apsp_auto_report",
     "fw_measure_relax_peak_packed",
+    "fw_apsp_paths_i32",
+    "fw_path_length_i32",
+    "fw_dense_from_csr_i32",
+    "fw_negative_cycle_i32",
     "fw_batch_pack_offsets",
     "fw_batch_plan_create",
     "fw_batch_plan_autotune",
@@ -111,6 +115,14 @@ def lib():
     L.fw_profile_end.restype = c_int
     L.fw_measure_relax_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak.restype = c_int
+    L.fw_apsp_paths_i32.argtypes = [vp, vp, i64, i64, vp]
+    L.fw_apsp_paths_i32.restype = c_int
+    L.fw_path_length_i32.argtypes = [vp, i64, i64, i64, vp, i64]
+    L.fw_path_length_i32.restype = c_int
+    L.fw_dense_from_csr_i32.argtypes = [vp, vp, vp, i64, vp, vp, vp]
+    L.fw_dense_from_csr_i32.restype = c_int
+    L.fw_negative_cycle_i32.argtypes = [vp, i64, i64, vp, vp]
+    L.fw_negative_cycle_i32.restype = c_int
     L.fw_measure_relax_peak_packed.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak_packed.restype = c_int
     L.fw_apsp_auto_report.argtypes = [vp, ctypes.POINTER(c_int)]
@@ -223,6 +235,35 @@ def measure_relax_peak_packed(stream=None) -> float:
     a = ctypes.c_double(0)
     _check(lib().fw_measure_relax_peak_packed(ctypes.byref(a), _stream(stream)))
     return a.value
+
+
+# ------------------------------------------------------ paths, graph I/O, checks
+def apsp_paths_i32(d_D, d_nh, n: int, batch: int = 1, stream=None) -> None:
+    """In-place int32 APSP that also writes next hops into d_nh (int32, same shape)."""
+    _check(lib().fw_apsp_paths_i32(_ptr(d_D), _ptr(d_nh), n, batch, _stream(stream)))
+
+
+def path(nh: np.ndarray, i: int, j: int) -> list[int]:
+    """Vertices of the recorded path i -> j ([] if unreachable), from a host next-hop matrix."""
+    nh = np.ascontiguousarray(nh, dtype=np.int32)
+    n = nh.shape[0]
+    buf = np.empty(n + 1, dtype=np.int32)
+    k = lib().fw_path_length_i32(nh.ctypes.data, n, i, j, buf.ctypes.data, n + 1)
+    if k < 0:
+        raise FwError(-k, lib().fw_last_error_string().decode())
+    return buf[:k].tolist()
+
+
+def dense_from_csr(d_rowptr, d_col, d_w, n: int, d_D, d_bad=None, stream=None) -> None:
+    """Dense int32 matrix (INF / 0 diagonal / min of duplicates) from a device CSR graph."""
+    _check(lib().fw_dense_from_csr_i32(_ptr(d_rowptr), _ptr(d_col) if d_col is not None else None,
+                                       _ptr(d_w) if d_w is not None else None, n, _ptr(d_D),
+                                       _ptr(d_bad) if d_bad is not None else None, _stream(stream)))
+
+
+def negative_cycle_flags(d_D, n: int, batch: int, d_flags, stream=None) -> None:
+    """d_flags[b] = 1 if graph b has a negative diagonal entry (hasNegativeCycle)."""
+    _check(lib().fw_negative_cycle_i32(_ptr(d_D), n, batch, _ptr(d_flags), _stream(stream)))
 
 
 # ----------------------------------------------------------------- batched APSP

@@ -49,7 +49,7 @@ ProfState g_prof;
 const char* const kClassNames[KC_COUNT] = {"fw_diag",          "fw_panel",        "fw_remainder",
                                            "fw_pivot_step",    "fw_batched",      "fw_forward_f32",
                                            "fw_backward_f32",  "fw_p16_diag",     "fw_p16_panel",
-                                           "fw_p16_remainder"};
+                                           "fw_p16_remainder", "fw_paths_i32"};
 
 cudaEvent_t prof_event() {
     if (g_prof.next == g_prof.pool.size()) {
@@ -217,6 +217,33 @@ int fw_apsp_auto_report(fw_stream_t stream, int* used_packed) {
     FW_CUDA_TRY(cudaMemcpy(&v, done, sizeof(v), cudaMemcpyDeviceToHost));
     *used_packed = v ? 1 : 0;
     return FW_OK;
+}
+
+int fw_apsp_paths_i32(int32_t* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream) {
+    if (!d_D || !d_nh) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_paths_i32: NULL pointer");
+    if (n < 1 || n > 65535 || batch < 1 || batch > 65535)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_paths_i32: need 1 <= n <= 65535 and 1 <= batch <= 65535");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    void* ws = workspace_get(s, f32_workspace_bytes(n, batch));
+    if (!ws) return FW_ERR_NO_MEMORY;
+    return i32_paths(d_D, d_nh, n, batch, ws, s);
+}
+
+int fw_path_length_i32(const int32_t* h_nh, int64_t n, int64_t i, int64_t j, int32_t* h_path, int64_t cap) {
+    if (!h_nh || n < 1 || i < 0 || j < 0 || i >= n || j >= n)
+        return -set_error(FW_ERR_INVALID_ARGUMENT, "fw_path_length_i32: bad arguments");
+    if (h_nh[i * n + j] < 0) return 0;
+    int64_t len = 0, u = i;
+    if (h_path && cap > 0) h_path[0] = (int32_t)i;
+    len = 1;
+    while (u != j) {
+        const int64_t v = h_nh[u * n + j];
+        if (v < 0 || v >= n || len > n) return -set_error(FW_ERR_INVALID_ARGUMENT, "next hops do not form a path");
+        if (h_path && len < cap) h_path[len] = (int32_t)v;
+        ++len;
+        u = v;
+    }
+    return (int)len;
 }
 
 int fw_forward_f32(float* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream) {

@@ -33,6 +33,27 @@ namespace fw {
 namespace {
 
 constexpr int kFThreads = 512;  // 16 row groups x 32 column groups
+
+// Value type of the next-hop sweep: fp32 (missing edge +inf) for the
+// differentiable form, int32 (missing edge INF = 1e9) for path reconstruction
+// of the integer sweep. INF + INF fits int32, so padded pivots never win.
+template <typename V>
+struct VT;
+template <>
+struct VT<float> {
+    __device__ static float inf() { return INFINITY; }
+    __device__ static bool edge(float v) { return isfinite(v); }
+};
+template <>
+struct VT<int> {
+    __device__ static int inf() { return kInf; }
+    __device__ static bool edge(int v) { return v < kInf; }
+};
+
+template <typename V>
+struct __align__(16) V4 {
+    V x, y, z, w;
+};
 constexpr int kFStages = 2;
 constexpr int kFSlabInts = kSlab * kTile;
 constexpr int kFStageInts = 3 * kFSlabInts;  // A values, A next hops, B values
@@ -40,19 +61,22 @@ constexpr int kFSmemBytes = kFStages * kFStageInts * 4;  // 96 KB
 
 // Thread (tx = t % 32, ty = t / 32) of a 128 x 128 tile owns rows
 // own_row(ty, r), r < 8, and columns tx*4 .. tx*4+3.
-__device__ __forceinline__ void relax_nh(float& c, int& h, float a, int ha, float b) {
-    const float s = a + b;
+template <typename V>
+__device__ __forceinline__ void relax_nh(V& c, int& h, V a, int ha, V b) {
+    const V s = a + b;
     if (s < c) {
         c = s;
         h = ha;
     }
 }
 
-__device__ __forceinline__ float4 ld4f(const float* p) { return *reinterpret_cast<const float4*>(p); }
+template <typename V>
+__device__ __forceinline__ V4<V> ld4v(const V* p) { return *reinterpret_cast<const V4<V>*>(p); }
 __device__ __forceinline__ int4 ld4i(const int* p) { return *reinterpret_cast<const int4*>(p); }
 
 // acc/nh for the 128 x 128 tile at (r0, c0) of an n x n matrix (inf / -1 outside).
-__device__ __forceinline__ void f_load_tile(float (&c)[8][4], int (&h)[8][4], const float* D, const int* nh,
+template <typename V>
+__device__ __forceinline__ void f_load_tile(V (&c)[8][4], int (&h)[8][4], const V* D, const int* nh,
                                             int64_t n, int64_t r0, int64_t c0, int tx, int ty) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -61,13 +85,14 @@ __device__ __forceinline__ void f_load_tile(float (&c)[8][4], int (&h)[8][4], co
         for (int e = 0; e < 4; ++e) {
             const int64_t j = c0 + tx * 4 + e;
             const bool in = i < n && j < n;
-            c[r][e] = in ? D[i * n + j] : INFINITY;
+            c[r][e] = in ? D[i * n + j] : VT<V>::inf();
             h[r][e] = in ? nh[i * n + j] : -1;
         }
     }
 }
 
-__device__ __forceinline__ void f_store_tile(const float (&c)[8][4], const int (&h)[8][4], float* D, int* nh, int64_t n,
+template <typename V>
+__device__ __forceinline__ void f_store_tile(const V (&c)[8][4], const int (&h)[8][4], V* D, int* nh, int64_t n,
                                              int64_t r0, int64_t c0, int tx, int ty) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -94,37 +119,40 @@ __device__ __forceinline__ void f_load_kmajor(void* dst, const void* buf, int64_
 }
 
 // Slab of D rows [r0, r0 + 32), columns [c0, c0 + 128) (inf outside).
-__device__ __forceinline__ void f_load_rows(float* dst, const float* D, int64_t n, int64_t r0, int64_t c0, int tid) {
+template <typename V>
+__device__ __forceinline__ void f_load_rows(V* dst, const V* D, int64_t n, int64_t r0, int64_t c0, int tid) {
     for (int q = tid; q < kSlab * kTile; q += kFThreads) {
         const int row = q >> 7, col = q & 127;
         const int64_t i = r0 + row, j = c0 + col;
-        dst[row * kTile + col] = (i < n && j < n) ? D[i * n + j] : INFINITY;
+        dst[row * kTile + col] = (i < n && j < n) ? D[i * n + j] : VT<V>::inf();
     }
 }
 
 // Transposed slab of D and nh: dst[kk][i] = X[r0 + i][k0 + kk].
-__device__ __forceinline__ void f_load_transposed(float* dv, int* dh, const float* D, const int* nh, int64_t n,
+template <typename V>
+__device__ __forceinline__ void f_load_transposed(V* dv, int* dh, const V* D, const int* nh, int64_t n,
                                                   int64_t r0, int64_t k0, int tid) {
     for (int q = tid; q < kTile * kSlab; q += kFThreads) {
         const int i = q >> 5, kk = q & 31;
         const int64_t gi = r0 + i, gk = k0 + kk;
         const bool in = gi < n && gk < n;
-        dv[kk * kTile + i] = in ? D[gi * n + gk] : INFINITY;
+        dv[kk * kTile + i] = in ? D[gi * n + gk] : VT<V>::inf();
         dh[kk * kTile + i] = in ? nh[gi * n + gk] : -1;
     }
 }
 
 // One slab: c/h = relax with A (values av, hops ah; k-major) and B (bv; k-major).
-__device__ __forceinline__ void f_relax_slab(float (&c)[8][4], int (&h)[8][4], const float* av, const int* ah,
-                                             const float* bv, int nk, int tx, int ty) {
+template <typename V>
+__device__ __forceinline__ void f_relax_slab(V (&c)[8][4], int (&h)[8][4], const V* av, const int* ah,
+                                             const V* bv, int nk, int tx, int ty) {
 #pragma unroll 2
     for (int kk = 0; kk < nk; ++kk) {
-        const float4 a0 = ld4f(av + kk * kTile + ty * 4), a1 = ld4f(av + kk * kTile + 64 + ty * 4);
+        const V4<V> a0 = ld4v(av + kk * kTile + ty * 4), a1 = ld4v(av + kk * kTile + 64 + ty * 4);
         const int4 h0 = ld4i(ah + kk * kTile + ty * 4), h1 = ld4i(ah + kk * kTile + 64 + ty * 4);
-        const float4 b = ld4f(bv + kk * kTile + tx * 4);
-        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const V4<V> b = ld4v(bv + kk * kTile + tx * 4);
+        const V a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const int ha[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
-        const float bb[4] = {b.x, b.y, b.z, b.w};
+        const V bb[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
         for (int r = 0; r < 8; ++r)
 #pragma unroll
@@ -133,59 +161,61 @@ __device__ __forceinline__ void f_relax_slab(float (&c)[8][4], int (&h)[8][4], c
 }
 
 // Two-stage pipeline over the pivot slabs: la(av, ah, s) / lb(bv, s) fill slab s.
-template <class LA, class LB>
-__device__ __forceinline__ void f_mainloop(float (&c)[8][4], int (&h)[8][4], int kv, int* smem, LA la, LB lb, int tx,
+template <typename V, class LA, class LB>
+__device__ __forceinline__ void f_mainloop(V (&c)[8][4], int (&h)[8][4], int kv, int* smem, LA la, LB lb, int tx,
                                            int ty) {
     const int nslab = (kv + kSlab - 1) / kSlab;
     auto stage = [&](int s) { return smem + (s % kFStages) * kFStageInts; };
     {
         int* st = stage(0);
-        la(reinterpret_cast<float*>(st), st + kFSlabInts, 0);
-        lb(reinterpret_cast<float*>(st + 2 * kFSlabInts), 0);
+        la(reinterpret_cast<V*>(st), st + kFSlabInts, 0);
+        lb(reinterpret_cast<V*>(st + 2 * kFSlabInts), 0);
         cp_async_commit();
     }
     for (int s = 0; s < nslab; ++s) {
         if (s + 1 < nslab) {
             int* st = stage(s + 1);
-            la(reinterpret_cast<float*>(st), st + kFSlabInts, s + 1);
-            lb(reinterpret_cast<float*>(st + 2 * kFSlabInts), s + 1);
+            la(reinterpret_cast<V*>(st), st + kFSlabInts, s + 1);
+            lb(reinterpret_cast<V*>(st + 2 * kFSlabInts), s + 1);
         }
         cp_async_commit();
         cp_async_wait<1>();
         __syncthreads();
         const int* st = stage(s);
         const int nk = min(kSlab, kv - s * kSlab);
-        f_relax_slab(c, h, reinterpret_cast<const float*>(st), st + kFSlabInts,
-                     reinterpret_cast<const float*>(st + 2 * kFSlabInts), nk, tx, ty);
+        f_relax_slab<V>(c, h, reinterpret_cast<const V*>(st), st + kFSlabInts,
+                        reinterpret_cast<const V*>(st + 2 * kFSlabInts), nk, tx, ty);
         __syncthreads();
     }
 }
 
 // Next hops of the input: j for an edge, i on the diagonal, -1 otherwise.
-__global__ void fw_nh_init_kernel(const float* __restrict__ D, int* __restrict__ nh, int64_t n, int64_t total) {
+template <typename V>
+__global__ void fw_nh_init_kernel(const V* __restrict__ D, int* __restrict__ nh, int64_t n, int64_t total) {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t e = q % (n * n);
         const int64_t i = e / n, j = e % n;
-        nh[q] = (i == j) ? (int)i : (isfinite(D[q]) ? (int)j : -1);
+        nh[q] = (i == j) ? (int)i : (VT<V>::edge(D[q]) ? (int)j : -1);
     }
 }
 
 // Phase 1: closure of the diagonal block of graph blockIdx.z; 512 threads,
 // 4 x 8 values + next hops each; also fills the workspace panels.
+template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
-    fw_f32_diag_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int64_t p0,
-                       float* __restrict__ colTall, int* __restrict__ colHall, float* __restrict__ rowPall) {
-    __shared__ __align__(16) float prow[2][kTile];
-    __shared__ __align__(16) float pcol[2][kTile];
+    fw_nh_diag_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int64_t p0,
+                      V* __restrict__ colTall, int* __restrict__ colHall, V* __restrict__ rowPall) {
+    __shared__ __align__(16) V prow[2][kTile];
+    __shared__ __align__(16) V pcol[2][kTile];
     __shared__ __align__(16) int pcolh[2][kTile];
     const int64_t gph = blockIdx.z;
-    float* D = Dall + gph * n * n;
+    V* D = Dall + gph * n * n;
     int* nh = nhall + gph * n * n;
-    float* colT = colTall + gph * kTile * ldp;
+    V* colT = colTall + gph * kTile * ldp;
     int* colH = colHall + gph * kTile * ldp;
-    float* rowP = rowPall + gph * kTile * ldp;
+    V* rowP = rowPall + gph * kTile * ldp;
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;  // rows ty*4.., columns tx*8..
-    float c[4][8];
+    V c[4][8];
     int h[4][8];
     const int64_t rem = n - p0;
 #pragma unroll
@@ -194,7 +224,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
         for (int e = 0; e < 8; ++e) {
             const int lr = ty * 4 + r, lc = tx * 8 + e;
             const bool in = lr < rem && lc < rem;
-            c[r][e] = in ? D[(p0 + lr) * n + p0 + lc] : INFINITY;
+            c[r][e] = in ? D[(p0 + lr) * n + p0 + lc] : VT<V>::inf();
             h[r][e] = in ? nh[(p0 + lr) * n + p0 + lc] : -1;
         }
     if (ty == 0)
@@ -211,7 +241,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int k = kb + u, buf = u & 1;
-            float a[4], b[8];
+            V a[4], b[8];
             int ha[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
@@ -256,31 +286,32 @@ __global__ void __launch_bounds__(kFThreads, 1)
 }
 
 // Phase 2: blockIdx.y == 0 -> row panel tile (P, J); == 1 -> column panel tile (I, P).
+template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
-    fw_f32_panel_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
-                        float* __restrict__ colTall, int* __restrict__ colHall, float* __restrict__ rowPall) {
+    fw_nh_panel_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
+                       V* __restrict__ colTall, int* __restrict__ colHall, V* __restrict__ rowPall) {
     extern __shared__ __align__(128) int smem[];
     const int64_t gph = blockIdx.z;
-    float* D = Dall + gph * n * n;
+    V* D = Dall + gph * n * n;
     int* nh = nhall + gph * n * n;
-    float* colT = colTall + gph * kTile * ldp;
+    V* colT = colTall + gph * kTile * ldp;
     int* colH = colHall + gph * kTile * ldp;
-    float* rowP = rowPall + gph * kTile * ldp;
+    V* rowP = rowPall + gph * kTile * ldp;
     const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     const int other = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
     const int64_t p0 = (int64_t)pt * kTile, q0 = (int64_t)other * kTile;
     const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
-    float c[8][4];
+    V c[8][4];
     int h[8][4];
     if (blockIdx.y == 0) {
         f_load_tile(c, h, D, nh, n, p0, q0, tx, ty);
         f_mainloop(
             c, h, kv, smem,
-            [&](float* av, int* ah, int s) {
+            [&](V* av, int* ah, int s) {
                 f_load_kmajor(av, colT, ldp, s * kSlab, p0, tid);
                 f_load_kmajor(ah, colH, ldp, s * kSlab, p0, tid);
             },
-            [&](float* bv, int s) { f_load_rows(bv, D, n, p0 + s * kSlab, q0, tid); }, tx, ty);
+            [&](V* bv, int s) { f_load_rows(bv, D, n, p0 + s * kSlab, q0, tid); }, tx, ty);
         f_store_tile(c, h, D, nh, n, p0, q0, tx, ty);
 #pragma unroll
         for (int r = 0; r < 8; ++r)
@@ -290,8 +321,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
         f_load_tile(c, h, D, nh, n, q0, p0, tx, ty);
         f_mainloop(
             c, h, kv, smem,
-            [&](float* av, int* ah, int s) { f_load_transposed(av, ah, D, nh, n, q0, p0 + s * kSlab, tid); },
-            [&](float* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, p0, tid); }, tx, ty);
+            [&](V* av, int* ah, int s) { f_load_transposed(av, ah, D, nh, n, q0, p0 + s * kSlab, tid); },
+            [&](V* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, p0, tid); }, tx, ty);
         f_store_tile(c, h, D, nh, n, q0, p0, tx, ty);
 #pragma unroll
         for (int r = 0; r < 8; ++r)
@@ -304,32 +335,33 @@ __global__ void __launch_bounds__(kFThreads, 1)
 }
 
 // Phase 3: remainder tile (I, J) of graph blockIdx.z.
+template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
-    fw_f32_remainder_kernel(float* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
-                            const float* __restrict__ colTall, const int* __restrict__ colHall,
-                            const float* __restrict__ rowPall) {
+    fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
+                           const V* __restrict__ colTall, const int* __restrict__ colHall,
+                           const V* __restrict__ rowPall) {
     extern __shared__ __align__(128) int smem[];
     const int64_t gph = blockIdx.z;
-    float* D = Dall + gph * n * n;
+    V* D = Dall + gph * n * n;
     int* nh = nhall + gph * n * n;
-    const float* colT = colTall + gph * kTile * ldp;
+    const V* colT = colTall + gph * kTile * ldp;
     const int* colH = colHall + gph * kTile * ldp;
-    const float* rowP = rowPall + gph * kTile * ldp;
+    const V* rowP = rowPall + gph * kTile * ldp;
     const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
     const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
     const int64_t p0 = (int64_t)pt * kTile, r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
     const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
-    float c[8][4];
+    V c[8][4];
     int h[8][4];
     f_load_tile(c, h, D, nh, n, r0, c0, tx, ty);
     f_mainloop(
         c, h, kv, smem,
-        [&](float* av, int* ah, int s) {
+        [&](V* av, int* ah, int s) {
             f_load_kmajor(av, colT, ldp, s * kSlab, r0, tid);
             f_load_kmajor(ah, colH, ldp, s * kSlab, r0, tid);
         },
-        [&](float* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, c0, tid); }, tx, ty);
+        [&](V* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, c0, tid); }, tx, ty);
     f_store_tile(c, h, D, nh, n, r0, c0, tx, ty);
 }
 
@@ -383,38 +415,48 @@ size_t f32_workspace_bytes(int64_t n, int64_t batch) {
     return (size_t)3 * kTile * ldp * 4 * (size_t)batch;
 }
 
-int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
+template <typename V>
+int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, KernelClass kc) {
     static bool attr_done = false;
     if (!attr_done) {
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_f32_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
         FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_f32_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+            cudaFuncSetAttribute(fw_nh_panel_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+        FW_CUDA_TRY(
+            cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
         attr_done = true;
     }
     const int T = (int)((n + kTile - 1) / kTile);
     const int64_t ldp = (int64_t)T * kTile;
-    float* colT = static_cast<float*>(ws);
+    V* colT = static_cast<V*>(ws);
     int* colH = reinterpret_cast<int*>(colT + (size_t)kTile * ldp * batch);
-    float* rowP = reinterpret_cast<float*>(colH + (size_t)kTile * ldp * batch);
+    V* rowP = reinterpret_cast<V*>(colH + (size_t)kTile * ldp * batch);
     const int64_t total = n * n * batch;
-    prof_begin(KC_FWD_F32, s);
-    fw_nh_init_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 4096), 256, 0, s>>>(D, nh, n, total);
+    prof_begin(kc, s);
+    fw_nh_init_kernel<V><<<(unsigned)std::min<int64_t>((total + 255) / 256, 4096), 256, 0, s>>>(D, nh, n, total);
     FW_LAUNCH_CHECK("fw_nh_init_kernel");
     for (int pt = 0; pt < T; ++pt) {
         const int64_t p0 = (int64_t)pt * kTile;
-        fw_f32_diag_kernel<<<dim3(1, 1, (unsigned)batch), kFThreads, 0, s>>>(D, nh, n, ldp, p0, colT, colH, rowP);
-        FW_LAUNCH_CHECK("fw_f32_diag_kernel");
+        fw_nh_diag_kernel<V><<<dim3(1, 1, (unsigned)batch), kFThreads, 0, s>>>(D, nh, n, ldp, p0, colT, colH, rowP);
+        FW_LAUNCH_CHECK("fw_nh_diag_kernel");
         if (T > 1) {
-            fw_f32_panel_kernel<<<dim3(T - 1, 2, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(D, nh, n, ldp, pt,
-                                                                                             colT, colH, rowP);
-            FW_LAUNCH_CHECK("fw_f32_panel_kernel");
-            fw_f32_remainder_kernel<<<dim3(T - 1, T - 1, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(
+            fw_nh_panel_kernel<V><<<dim3(T - 1, 2, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(D, nh, n, ldp, pt,
+                                                                                               colT, colH, rowP);
+            FW_LAUNCH_CHECK("fw_nh_panel_kernel");
+            fw_nh_remainder_kernel<V><<<dim3(T - 1, T - 1, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(
                 D, nh, n, ldp, pt, colT, colH, rowP);
-            FW_LAUNCH_CHECK("fw_f32_remainder_kernel");
+            FW_LAUNCH_CHECK("fw_nh_remainder_kernel");
         }
     }
-    prof_end(KC_FWD_F32, s, (double)n * n * n * batch);
+    prof_end(kc, s, (double)n * n * n * batch);
     return FW_OK;
+}
+
+int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
+    return nh_forward<float>(D, nh, n, batch, ws, s, KC_FWD_F32);
+}
+
+int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
+    return nh_forward<int>(D, nh, n, batch, ws, s, KC_PATHS_I32);
 }
 
 int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s) {

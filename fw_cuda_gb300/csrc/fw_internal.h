@@ -41,6 +41,7 @@ enum KernelClass {
     KC_P16_DIAG,
     KC_P16_PANEL,
     KC_P16_REMAINDER,
+    KC_PATHS_I32,
     KC_COUNT
 };
 
@@ -74,6 +75,8 @@ int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 size_t f32_workspace_bytes(int64_t n, int64_t batch);
 int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
 int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s);
+// int32 sweep that also records next hops (same kernels as the fp32 form).
+int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
 
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);

@@ -89,6 +89,40 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
  * address (cudaGetSymbolAddress); make it before any stream capture. */
 int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
 
+/* ---------------------------------------------------------------- path reconstruction */
+
+/* int32 APSP that also records next hops, for `batch` equal-size graphs
+ * (stride n*n): d_D as in fw_apsp_i32 (same distances, bit for bit), d_nh[i][j]
+ * = the vertex after i on a shortest path to j (j for a direct edge when no
+ * shorter path exists, i on the diagonal, -1 when j is unreachable), updated
+ * on strict improvement as nh[i][j] = nh[i][k]. No counterpart in the
+ * reference (its sweeps keep distances only). */
+int fw_apsp_paths_i32(int32_t* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream);
+
+/* Host helper: walks a next-hop matrix (host copy) from i to j, writing up to
+ * `cap` vertices (i first, j last) into h_path; returns the number of
+ * vertices on the path, 0 when j is unreachable, a negative fw_status-like
+ * error (sets the last error) when the next hops do not form a path. */
+int fw_path_length_i32(const int32_t* h_nh, int64_t n, int64_t i, int64_t j, int32_t* h_path, int64_t cap);
+
+/* ---------------------------------------------------------------- graph I/O, checks */
+
+/* Dense n x n int32 matrix from a CSR adjacency on the device (d_rowptr: n+1
+ * monotone offsets, d_col / d_w: rowptr[n] column indices and int32 weights),
+ * in the reference's convention: FW_INF where there is no edge, 0 on the
+ * diagonal (a negative self-loop lowers it), the smallest weight among
+ * duplicate edges. Edges with a column outside [0, n) or a weight >= FW_INF
+ * are skipped and counted into *d_bad when d_bad is not NULL. With d_col or
+ * d_w NULL only the empty graph is written. No counterpart in the reference
+ * (its generator is dense and on the host, src/graph_generator.cpp:7-46). */
+int fw_dense_from_csr_i32(const int64_t* d_rowptr, const int32_t* d_col, const int32_t* d_w, int64_t n,
+                          int32_t* d_D, uint32_t* d_bad, fw_stream_t stream);
+
+/* d_flags[b] = 1 if graph b (of `batch` equal-size n x n graphs, stride n*n)
+ * has a negative diagonal entry after the sweep, else 0: the reference's
+ * hasNegativeCycle (src/utils.cpp:5-12) on the device. */
+int fw_negative_cycle_i32(const int32_t* d_D, int64_t n, int64_t batch, int32_t* d_flags, fw_stream_t stream);
+
 /* ---------------------------------------------------------------- batched APSP */
 
 /* Many independent graphs solved in one persistent launch. No counterpart in
