@@ -136,20 +136,6 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// Tile index sets of the remainder launches: either every tile index except
-// up to two excluded ones (ex0 < ex1, -1 = none), or one single index.
-struct TileSet {
-    int single;  // >= 0: the only index; -1: all but the excluded ones
-    int ex0, ex1;
-};
-
-__device__ __forceinline__ int tile_of(const TileSet& s, int idx) {
-    if (s.single >= 0) return s.single;
-    if (s.ex0 >= 0 && idx >= s.ex0) ++idx;
-    if (s.ex1 >= 0 && idx >= s.ex1) ++idx;
-    return idx;
-}
-
 // Phase 3: tiles (I, J), I from `rows`, J from `cols`:
 // D[I][J] = min(D[I][J], colT[k][I]^T (x) rowP[k][J]) over workspace pivot
 // rows k in [slab0 * 32, (slab0 + nslab) * 32).
@@ -218,13 +204,6 @@ __global__ void __launch_bounds__(256)
         }
     }
 }
-
-TileSet all_but(int a, int b = -1) {
-    if (b >= 0 && b < a) std::swap(a, b);
-    if (a < 0) std::swap(a, b);
-    return TileSet{-1, a, b};
-}
-TileSet only(int t) { return TileSet{t, -1, -1}; }
 
 template <bool VEC>
 struct Blocked {

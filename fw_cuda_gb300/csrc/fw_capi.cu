@@ -120,6 +120,25 @@ void* workspace_get(cudaStream_t s, size_t bytes) {
     return p;
 }
 
+namespace {
+std::mutex g_aux_mutex;
+std::map<std::pair<int, cudaStream_t>, AuxStream> g_aux;
+}  // namespace
+
+int aux_stream_get(cudaStream_t s, AuxStream* out) {
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_aux_mutex);
+    AuxStream& a = g_aux[{dev, s}];
+    if (!a.side) {
+        FW_CUDA_TRY(cudaStreamCreateWithFlags(&a.side, cudaStreamNonBlocking));
+        FW_CUDA_TRY(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
+        FW_CUDA_TRY(cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming));
+    }
+    *out = a;
+    return FW_OK;
+}
+
 int normalise_kappa(int kappa) { return (kappa <= 0 || kappa > 16) ? 4 : kappa; }
 
 }  // namespace fw

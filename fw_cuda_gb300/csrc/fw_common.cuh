@@ -150,6 +150,34 @@ __device__ __forceinline__ void st_vec(int* p, const int (&v)[R]) {
     }
 }
 
+// Tile index sets of the remainder launches: either every tile index except
+// up to two excluded ones (ex0 < ex1, -1 = none), or one single index.
+struct TileSet {
+    int single;  // >= 0: the only index; -1: all but the excluded ones
+    int ex0, ex1;
+};
+
+__device__ __forceinline__ int tile_of(const TileSet& s, int idx) {
+    if (s.single >= 0) return s.single;
+    if (s.ex0 >= 0 && idx >= s.ex0) ++idx;
+    if (s.ex1 >= 0 && idx >= s.ex1) ++idx;
+    return idx;
+}
+
+inline TileSet all_but(int a, int b = -1) {
+    if (b >= 0 && b < a) {
+        const int t = a;
+        a = b;
+        b = t;
+    }
+    if (a < 0) {
+        a = b;
+        b = -1;
+    }
+    return TileSet{-1, a, b};
+}
+inline TileSet only(int t) { return TileSet{t, -1, -1}; }
+
 // ------------------------------------------------------------ block closure
 // Min-plus closure (the k-sequential Floyd-Warshall sweep) of an NB x NB block
 // held in registers by a TY x TX grid of threads, each owning rows

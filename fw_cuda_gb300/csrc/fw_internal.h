@@ -55,6 +55,17 @@ void prof_end(KernelClass kc, cudaStream_t s, double relaxations);
 // error) when allocation fails.
 void* workspace_get(cudaStream_t s, size_t bytes);
 
+// A second, non-blocking stream and a fork / join event pair tied to the
+// caller's (device, stream), created on first use and kept: the look-ahead
+// schedules run the bulk remainder of one pivot block on the side stream while
+// the next block is closed on the caller's stream.
+struct AuxStream {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join = nullptr;
+};
+int aux_stream_get(cudaStream_t s, AuxStream* out);
+
 // Normalised arguments of the blocked sweep.
 int normalise_kappa(int kappa);
 

@@ -369,16 +369,17 @@ __global__ void __launch_bounds__(kPThreads, 1)
     }
 }
 
-// Remainder tile (I, J), both different from the pivot block.
+// Remainder tiles (I, J), I from `rows`, J from `cols`, with the 256 pivots of
+// the panels in colD / rowP.
 __global__ void __launch_bounds__(kPThreads, 1)
-    fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, int pt, const uint32_t* __restrict__ colD,
-                            const uint32_t* __restrict__ rowP, const P16Status* st, int one) {
+    fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, TileSet rows, TileSet cols,
+                            const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP, const P16Status* st,
+                            int one) {
     if (st->ineligible) return;
     extern __shared__ __align__(128) uint32_t psm[];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
-    const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
-    const int64_t r0 = (int64_t)ti * kPT, w0 = (int64_t)tj * kPW, ldw = ld16 / 2;
+    const int64_t r0 = (int64_t)tile_of(rows, blockIdx.y) * kPT, w0 = (int64_t)tile_of(cols, blockIdx.x) * kPW;
+    const int64_t ldw = ld16 / 2;
     uint32_t c[8][8];
     p_load_tile(c, D16, ldw, r0, w0, tx, ty);
     p_mainloop(
@@ -395,13 +396,17 @@ size_t p16_workspace_bytes(int64_t n) {
     const int64_t ld = p16_ld(n);
     return 256                                   // status
            + (size_t)ld * ld * 2                 // D16
-           + (size_t)kPT * ld * 4                // colD (duplicated words)
-           + (size_t)kPT * (ld / 2) * 4;         // rowP (packed words)
+           + 2 * ((size_t)kPT * ld * 4           // colD (duplicated words), two stage buffers
+                  + (size_t)kPT * (ld / 2) * 4); // rowP (packed words), two stage buffers
 }
 
-// Enqueues encode, the packed sweep and the guarded decode; *status_out
-// receives the device address of the status word whose `done` field tells
-// the int32 kernels to skip.
+// Enqueues encode, the packed sweep and the guarded decode on `s`; *done_flag
+// receives the device address of the word that tells the int32 kernels to
+// skip. The sweep looks one pivot block ahead: after block t's panels, the
+// tiles of block t+1's row and column get block t's update on `s`, then the
+// other remainder tiles of block t run on a side stream while block t+1 is
+// closed and its panels computed on `s` (into the other panel buffer); `s`
+// waits for the side stream before block t+1's own remainder.
 int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
     static bool attr_done = false;
     if (!attr_done) {
@@ -410,13 +415,19 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
             cudaFuncSetAttribute(fw_p16_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
         attr_done = true;
     }
+    AuxStream aux;
+    if (int rc = aux_stream_get(s, &aux)) return rc;
     const int64_t ld = p16_ld(n);
     const int T = (int)(ld / kPT);
     char* base = static_cast<char*>(ws);
     P16Status* st = reinterpret_cast<P16Status*>(base);
     uint16_t* D16 = reinterpret_cast<uint16_t*>(base + 256);
-    uint32_t* colD = reinterpret_cast<uint32_t*>(base + 256 + (size_t)ld * ld * 2);
-    uint32_t* rowP = colD + (size_t)kPT * ld;
+    uint32_t* colD[2];
+    uint32_t* rowP[2];
+    colD[0] = reinterpret_cast<uint32_t*>(base + 256 + (size_t)ld * ld * 2);
+    rowP[0] = colD[0] + (size_t)kPT * ld;
+    colD[1] = rowP[0] + (size_t)kPT * (ld / 2);
+    rowP[1] = colD[1] + (size_t)kPT * ld;
     FW_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(P16Status), s));
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -424,23 +435,57 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
     const unsigned grid = (unsigned)(sms > 0 ? sms * 8 : 1024);
     fw_p16_encode_kernel<<<grid, 256, 0, s>>>(D, n, D16, ld, st);
     FW_LAUNCH_CHECK("fw_p16_encode_kernel");
-    for (int pt = 0; pt < T; ++pt) {
-        const double kv = (double)((n - (int64_t)pt * kPT) < kPT ? n - (int64_t)pt * kPT : kPT);
-        prof_begin(KC_P16_DIAG, s);
-        fw_p16_diag_kernel<<<1, kPThreads, 0, s>>>(D16, ld, (int64_t)pt * kPT, colD, rowP, st);
+
+    auto kv = [&](int t) { return (double)((n - (int64_t)t * kPT) < kPT ? n - (int64_t)t * kPT : kPT); };
+    auto close = [&](int t, cudaStream_t q) -> int {
+        const int b = t & 1;
+        prof_begin(KC_P16_DIAG, q);
+        fw_p16_diag_kernel<<<1, kPThreads, 0, q>>>(D16, ld, (int64_t)t * kPT, colD[b], rowP[b], st);
         FW_LAUNCH_CHECK("fw_p16_diag_kernel");
-        prof_end(KC_P16_DIAG, s, kv * kv * kv);
+        prof_end(KC_P16_DIAG, q, kv(t) * kv(t) * kv(t));
         if (T > 1) {
-            prof_begin(KC_P16_PANEL, s);
-            fw_p16_panel_kernel<<<dim3(T - 1, 2), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st, 1);
+            prof_begin(KC_P16_PANEL, q);
+            fw_p16_panel_kernel<<<dim3(T - 1, 2), kPThreads, kPSmemBytes, q>>>(D16, ld, t, colD[b], rowP[b], st, 1);
             FW_LAUNCH_CHECK("fw_p16_panel_kernel");
-            prof_end(KC_P16_PANEL, s, 2.0 * ((double)n - kv) * kv * kv);
-            prof_begin(KC_P16_REMAINDER, s);
-            fw_p16_remainder_kernel<<<dim3(T - 1, T - 1), kPThreads, kPSmemBytes, s>>>(D16, ld, pt, colD, rowP, st,
-                                                                                        1);
-            FW_LAUNCH_CHECK("fw_p16_remainder_kernel");
-            prof_end(KC_P16_REMAINDER, s, ((double)n - kv) * ((double)n - kv) * kv);
+            prof_end(KC_P16_PANEL, q, 2.0 * ((double)n - kv(t)) * kv(t) * kv(t));
         }
+        return FW_OK;
+    };
+    auto rows_of = [&](const TileSet& ts) {
+        if (ts.single >= 0) return kv(ts.single);
+        double r = (double)n;
+        if (ts.ex0 >= 0) r -= kv(ts.ex0);
+        if (ts.ex1 >= 0) r -= kv(ts.ex1);
+        return r;
+    };
+    auto remainder = [&](int t, TileSet rows, int nrows, TileSet cols, int ncols, cudaStream_t q) -> int {
+        if (nrows <= 0 || ncols <= 0) return FW_OK;
+        const int b = t & 1;
+        prof_begin(KC_P16_REMAINDER, q);
+        fw_p16_remainder_kernel<<<dim3(ncols, nrows), kPThreads, kPSmemBytes, q>>>(D16, ld, rows, cols, colD[b],
+                                                                                  rowP[b], st, 1);
+        FW_LAUNCH_CHECK("fw_p16_remainder_kernel");
+        prof_end(KC_P16_REMAINDER, q, rows_of(rows) * rows_of(cols) * kv(t));
+        return FW_OK;
+    };
+
+    if (int rc = close(0, s)) return rc;
+    for (int t = 0; t < T; ++t) {
+        if (t + 1 >= T) {
+            if (int rc = remainder(t, all_but(t), T - 1, all_but(t), T - 1, s)) return rc;
+            break;
+        }
+        // block t's update of block t+1's row (all columns but t) and column
+        if (int rc = remainder(t, only(t + 1), 1, all_but(t), T - 1, s)) return rc;
+        if (int rc = remainder(t, all_but(t, t + 1), T - 2, only(t + 1), 1, s)) return rc;
+        // the rest of block t's remainder on the side stream ...
+        FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+        if (int rc = remainder(t, all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, aux.side)) return rc;
+        FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
+        // ... while block t+1 is closed on the caller's stream
+        if (int rc = close(t + 1, s)) return rc;
+        FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
     }
     fw_p16_rmax_kernel<<<grid, 256, 0, s>>>(D16, n, ld, st);
     FW_LAUNCH_CHECK("fw_p16_rmax_kernel");

@@ -95,8 +95,11 @@ int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int varian
  * (stride n*n): d_D as in fw_apsp_i32 (same distances, bit for bit), d_nh[i][j]
  * = the vertex after i on a shortest path to j (j for a direct edge when no
  * shorter path exists, i on the diagonal, -1 when j is unreachable), updated
- * on strict improvement as nh[i][j] = nh[i][k]. No counterpart in the
- * reference (its sweeps keep distances only). */
+ * on strict improvement as nh[i][j] = nh[i][k]. The distances are exact for
+ * any graph without negative cycles; the next hops spell out shortest paths
+ * when every cycle has positive weight (with zero-weight cycles, equal-length
+ * alternatives can make recorded first hops point around such a cycle). No
+ * counterpart in the reference (its sweeps keep distances only). */
 int fw_apsp_paths_i32(int32_t* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_stream_t stream);
 
 /* Host helper: walks a next-hop matrix (host copy) from i to j, writing up to

@@ -34,7 +34,8 @@ def walk_all(W: np.ndarray, D: np.ndarray, nh: np.ndarray) -> None:
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 7, 130, 300, 1000])
 def test_int_paths(fw, cuda, oracle, n):
-    W = oracle.generate_graph(n, 0.1 if n > 100 else 0.4, 10 + n, 0, 100)
+    # positive weights: every cycle is positive, so recorded paths must end
+    W = oracle.generate_graph(n, 0.1 if n > 100 else 0.4, 10 + n, 1, 100)
     d = cuda.from_numpy(W).cuda()
     nh = cuda.empty_like(d)
     fw.apsp_paths_i32(d, nh, n)
@@ -50,7 +51,8 @@ def test_int_paths_batch_and_negative_weights(fw, cuda, oracle):
     n, B = 200, 5
     Ws = []
     for b in range(B):
-        W = oracle.generate_graph(n, 0.2, 300 + b, 0, 50).astype(np.int64)
+        # a potential shift keeps every cycle's (positive) weight: negative edges, no zero cycles
+        W = oracle.generate_graph(n, 0.2, 300 + b, 1, 50).astype(np.int64)
         p = rng.integers(0, 30, n)
         W = np.where(W < INF, W + p[:, None] - p[None, :], INF)
         np.fill_diagonal(W, 0)
@@ -64,6 +66,17 @@ def test_int_paths_batch_and_negative_weights(fw, cuda, oracle):
         D = d[b].cpu().numpy()
         assert np.array_equal(D, oracle.fw_i32(Ws[b]))
         walk_all(Ws[b], D, nh[b].cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_zero_weight_cycles_keep_exact_distances(fw, cuda, oracle):
+    """Zero-weight cycles: distances stay exact (next hops are only promised for positive cycles)."""
+    n = 300
+    W = oracle.generate_graph(n, 0.3, 17, 0, 3)  # many zero-weight edges and cycles
+    d = cuda.from_numpy(W).cuda()
+    nh = cuda.empty_like(d)
+    fw.apsp_paths_i32(d, nh, n)
+    assert np.array_equal(d.cpu().numpy(), oracle.fw_i32(W))
 
 
 @pytest.mark.gpu
