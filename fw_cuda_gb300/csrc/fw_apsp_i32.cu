@@ -214,6 +214,7 @@ struct Blocked {
     int* rowP;
     cudaStream_t s;
     const unsigned* skip;
+    AuxStream aux{};
 
     int64_t p0(int t) const { return (int64_t)t * kTile; }
     int64_t kv(int t) const { return n - p0(t) < kTile ? n - p0(t) : kTile; }
@@ -239,15 +240,17 @@ struct Blocked {
     }
     // Remainder launch over rows x cols with pivots [k_begin, k_end) of the
     // workspace (k_end - k_begin valid pivots; slabs rounded up).
-    int remainder(TileSet rows, int nrows, TileSet cols, int ncols, int k_begin, int k_valid) {
+    int remainder(TileSet rows, int nrows, TileSet cols, int ncols, int k_begin, int k_valid,
+                  cudaStream_t q = nullptr) {
         if (nrows <= 0 || ncols <= 0 || k_valid <= 0) return FW_OK;
+        if (q == nullptr) q = s;
         const int slab0 = k_begin / kSlab;
         const int nslab = (k_valid + kSlab - 1) / kSlab;
-        prof_begin(KC_REMAINDER, s);
-        fw_remainder_kernel<VEC><<<dim3(ncols, nrows), kThreads, kSmemBytes, s>>>(D, n, ldp, rows, cols, slab0, nslab,
+        prof_begin(KC_REMAINDER, q);
+        fw_remainder_kernel<VEC><<<dim3(ncols, nrows), kThreads, kSmemBytes, q>>>(D, n, ldp, rows, cols, slab0, nslab,
                                                                                  colT, rowP, 1, skip);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
-        prof_end(KC_REMAINDER, s, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
+        prof_end(KC_REMAINDER, q, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
         return FW_OK;
     }
     // Number of matrix rows (or columns) the tile set covers.
@@ -258,6 +261,32 @@ struct Blocked {
         if (ts.ex0 >= 0) r -= (double)kv(ts.ex0);
         if (ts.ex1 >= 0) r -= (double)kv(ts.ex1);
         return r;
+    }
+
+    // One 128-wide pivot block per remainder pass with a one-block look-ahead
+    // (tiling_gpu; kappa <= 4; needs two panel buffers): after block t's
+    // panels, block t's update of block t+1's row and column runs on the
+    // caller's stream, the rest of block t's remainder on the side stream
+    // while block t+1 is closed into the other panel buffer.
+    int lookahead() {
+        if (int rc = aux_stream_get(s, &aux)) return rc;
+        if (int rc = diag(0, 0)) return rc;
+        if (int rc = panels(0, 0)) return rc;
+        for (int t = 0; t < T; ++t) {
+            const int h = t & 1;
+            const int k0 = h * kTile, kvt = (int)kv(t);
+            if (t + 1 >= T) return remainder(all_but(t), T - 1, all_but(t), T - 1, k0, kvt);
+            if (int rc = remainder(only(t + 1), 1, all_but(t), T - 1, k0, kvt)) return rc;
+            if (int rc = remainder(all_but(t, t + 1), T - 2, only(t + 1), 1, k0, kvt)) return rc;
+            FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
+            FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+            if (int rc = remainder(all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, k0, kvt, aux.side)) return rc;
+            FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
+            if (int rc = diag(t + 1, h ^ 1)) return rc;
+            if (int rc = panels(t + 1, h ^ 1)) return rc;
+            FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
+        }
+        return FW_OK;
     }
 
     // One 128-wide pivot block per remainder pass (tiling_gpu; kappa <= 4).
@@ -294,8 +323,8 @@ struct Blocked {
 };
 
 template <bool VEC>
-int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, int* rowP, cudaStream_t s,
-                       const unsigned* skip) {
+int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahead, int* colT, int* rowP,
+                       cudaStream_t s, const unsigned* skip) {
     static bool attr_done = false;
     if (!attr_done) {
         FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
@@ -305,6 +334,7 @@ int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, int* colT, in
     }
     Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip};
     b.ldp = (int64_t)b.T * kTile;
+    if (blocks_per_pass == 1 && lookahead && b.T > 2) return b.lookahead();
     for (int t = 0; t < b.T;) {
         if (blocks_per_pass == 2 && t + 1 < b.T) {
             if (int rc = b.pair(t)) return rc;
@@ -330,13 +360,17 @@ size_t blocked_workspace_bytes(int64_t n, int blocks) {
     return (size_t)2 * blocks * kTile * (size_t)(T * kTile) * sizeof(int);
 }
 
-int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, cudaStream_t s, const unsigned int* skip) {
+int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, size_t ws_bytes, cudaStream_t s,
+                  const unsigned int* skip) {
     const int64_t T = (n + kTile - 1) / kTile;
+    // Two panel buffers are needed by the two-block pass and by the look-ahead.
+    const bool two = ws_bytes >= blocked_workspace_bytes(n, 2);
+    const int sets = two ? 2 : 1;
     int* colT = static_cast<int*>(ws);
-    int* rowP = colT + (size_t)blocks * kTile * (size_t)(T * kTile);
+    int* rowP = colT + (size_t)sets * kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    return vec ? blocked_solve_impl<true>(D, n, blocks, colT, rowP, s, skip)
-               : blocked_solve_impl<false>(D, n, blocks, colT, rowP, s, skip);
+    return vec ? blocked_solve_impl<true>(D, n, blocks, two, colT, rowP, s, skip)
+               : blocked_solve_impl<false>(D, n, blocks, two, colT, rowP, s, skip);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }

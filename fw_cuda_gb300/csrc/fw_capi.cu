@@ -171,21 +171,37 @@ const char* fw_last_error_string(void) { return t_last_error.c_str(); }
 
 const char* fw_version(void) { return "fw103 0.1.0 (sm_103a)"; }
 
+// The blocked variants run fastest with two panel buffers (look-ahead, or the
+// two-block pass of kappa > 4); one buffer is the minimum for kappa <= 4.
 size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     (void)tile;
     (void)kappa;
     if (n < 1) return 0;
     if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
-    const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
+    const size_t blocked = blocked_workspace_bytes(n, 2);
     if (variant == FW_VARIANT_AUTO) return ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
     return blocked;
 }
+
+}  // extern "C"
+
+namespace fw {
+size_t min_workspace_bytes(int64_t n, int kappa, int variant) {
+    if (n < 1) return 0;
+    if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
+    const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
+    if (variant == FW_VARIANT_AUTO) return ((blocked_workspace_bytes(n, 2) + 255) & ~size_t(255)) + p16_workspace_bytes(n);
+    return blocked;
+}
+}  // namespace fw
+
+extern "C" {
 
 int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
                    size_t workspace_bytes, fw_stream_t stream) {
     if (int rc = check_apsp_args(d_D, n, variant)) return rc;
     (void)tile;  // fixed geometry, as in the reference (src/fw_tiling_gpu.cu:254-257)
-    const size_t need = fw_workspace_bytes_i32(n, tile, kappa, variant);
+    const size_t need = min_workspace_bytes(n, kappa, variant);
     if (d_workspace == nullptr || workspace_bytes < need)
         return set_error(FW_ERR_INVALID_ARGUMENT,
                          "workspace of " + std::to_string(need) + " bytes required, got " +
@@ -196,7 +212,7 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
     if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
     const int blocks = blocks_per_pass(variant, kappa);
     if (variant == FW_VARIANT_AUTO) {
-        const size_t blocked = (blocked_workspace_bytes(n, blocks) + 255) & ~size_t(255);
+        const size_t blocked = (blocked_workspace_bytes(n, 2) + 255) & ~size_t(255);
         const unsigned int* done = nullptr;
         if (int rc = p16_solve(d_D, n, static_cast<char*>(d_workspace) + blocked, s, &done)) return rc;
         {
@@ -205,9 +221,9 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
             std::lock_guard<std::mutex> lk(g_ws_mutex);
             g_auto_done[{dev, s}] = done;
         }
-        return blocked_solve(d_D, n, blocks, d_workspace, s, done);
+        return blocked_solve(d_D, n, blocks, d_workspace, blocked, s, done);
     }
-    return blocked_solve(d_D, n, blocks, d_workspace, s);
+    return blocked_solve(d_D, n, blocks, d_workspace, workspace_bytes, s);
 }
 
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {

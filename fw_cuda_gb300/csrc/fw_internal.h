@@ -74,7 +74,12 @@ int blocks_per_pass(int variant, int kappa);
 size_t blocked_workspace_bytes(int64_t n, int blocks);
 // `skip`, when not null, is a device flag: nonzero makes every kernel of the
 // sweep return at once (the packed fast path already produced the result).
-int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, cudaStream_t s, const unsigned int* skip = nullptr);
+// With ws_bytes >= blocked_workspace_bytes(n, 2) the single-block schedule
+// runs with a one-block look-ahead (two panel buffers).
+int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, size_t ws_bytes, cudaStream_t s,
+                  const unsigned int* skip = nullptr);
+// Smallest workspace fw_apsp_i32_ws accepts for these arguments.
+size_t min_workspace_bytes(int64_t n, int kappa, int variant);
 
 // Exact packed 16-bit fast path (fw_packed16.cu).
 size_t p16_workspace_bytes(int64_t n);

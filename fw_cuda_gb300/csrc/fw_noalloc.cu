@@ -75,12 +75,14 @@ extern "C" int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa,
                              "fw_apsp_i32_noalloc: n = " + std::to_string(n) +
                                  " exceeds the fixed scratch limit of n <= " + std::to_string(kNoAllocMaxN) +
                                  "; use fw_apsp_i32 or fw_apsp_i32_ws for larger graphs");
-    const size_t need = fw_workspace_bytes_i32(n, tile, kappa, variant);
+    const size_t need = fw::min_workspace_bytes(n, kappa, variant);
     if (need > sizeof(g_fw_noalloc_scratch))
         return fw::set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_i32_noalloc: workspace of " + std::to_string(need) +
                                                           " bytes exceeds the fixed scratch array");
     if (d_D == nullptr) return fw::set_error(FW_ERR_INVALID_ARGUMENT, "d_D is NULL");
     void* scratch = nullptr;
     if (int rc = scratch_address(&scratch)) return rc;
-    return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, sizeof(g_fw_noalloc_scratch), stream);
+    // Passing exactly the minimum keeps the single-stream schedule (the
+    // look-ahead would also create a side stream on first use).
+    return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, need, stream);
 }

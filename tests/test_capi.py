@@ -55,7 +55,7 @@ def test_bad_arguments_fail_before_any_device_work(fw):
     need = L.fw_workspace_bytes_i32(1000, 32, 4, 2)
     assert need > 0
     assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, None, need, None) == fw.FW_ERR_INVALID_ARGUMENT
-    assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake, need - 1, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake, 4096, None) == fw.FW_ERR_INVALID_ARGUMENT
     assert b"workspace" in L.fw_last_error_string()
     assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake + 16, need, None) == fw.FW_ERR_INVALID_ARGUMENT
     # the per-pivot sweep puts one row per grid row
@@ -63,13 +63,12 @@ def test_bad_arguments_fail_before_any_device_work(fw):
 
 
 def test_workspace_sizes(fw):
-    # blocked: two 128-row panels with the leading dimension padded to 128
-    assert fw.workspace_bytes_i32(1, variant=1) == 2 * 128 * 128 * 4
-    assert fw.workspace_bytes_i32(32768, variant=2) == 2 * 128 * 32768 * 4
-    assert fw.workspace_bytes_i32(32769, variant=2) == 2 * 128 * (32768 + 128) * 4
-    # kappa > 4: two 128-wide pivot blocks per remainder pass, twice the panels
-    assert fw.workspace_bytes_i32(32768, kappa=8, variant=2) == 2 * 256 * 32768 * 4
-    assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == 2 * 128 * 32768 * 4
+    # blocked: two buffers of two 128-row panels (look-ahead or the two-block
+    # pass), leading dimension padded to 128
+    assert fw.workspace_bytes_i32(1, variant=1) == 2 * 256 * 128 * 4
+    assert fw.workspace_bytes_i32(32768, variant=2) == 2 * 256 * 32768 * 4
+    assert fw.workspace_bytes_i32(32769, variant=2) == 2 * 256 * (32768 + 128) * 4
+    assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == 2 * 256 * 32768 * 4
     # per-pivot: two row and two column snapshots
     assert fw.workspace_bytes_i32(1001, variant=0) == 4 * 1004 * 4
     assert fw.workspace_bytes_i32(0, variant=1) == 0

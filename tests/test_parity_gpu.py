@@ -153,10 +153,13 @@ def test_workspace_variant_matches(fw, cuda, oracle):
     ref = oracle.fw_i32(W)
     need = fw.workspace_bytes_i32(n, variant=2)
     ws = cuda.empty(need // 4 + 64, dtype=cuda.int32, device="cuda")
-    d = cuda.from_numpy(W).cuda()
-    fw.apsp_i32_ws(d, n, ws, need, variant=2)
-    cuda.cuda.synchronize()
-    assert np.array_equal(d.cpu().numpy(), ref)
+    # full size: look-ahead schedule; half: the minimum, one panel buffer
+    for nbytes in (need, need // 2):
+        for v in (1, 2):
+            d = cuda.from_numpy(W).cuda()
+            fw.apsp_i32_ws(d, n, ws, nbytes, variant=v)
+            cuda.cuda.synchronize()
+            assert np.array_equal(d.cpu().numpy(), ref), (nbytes, v)
 
 
 def test_stream_argument(fw, cuda, oracle):
