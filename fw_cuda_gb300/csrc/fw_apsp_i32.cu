@@ -220,22 +220,24 @@ struct Blocked {
     int64_t kv(int t) const { return n - p0(t) < kTile ? n - p0(t) : kTile; }
 
     // Diagonal closure of block t, its panels written to workspace half h.
-    int diag(int t, int h) {
-        prof_begin(KC_DIAG, s);
-        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, s>>>(D, n, ldp, p0(t), colT + h * kTile * ldp, rowP + h * kTile * ldp,
+    int diag(int t, int h, cudaStream_t q = nullptr) {
+        if (q == nullptr) q = s;
+        prof_begin(KC_DIAG, q);
+        fw_diag_kernel<VEC><<<1, kDiagThreads, 0, q>>>(D, n, ldp, p0(t), colT + h * kTile * ldp, rowP + h * kTile * ldp,
                                                        skip);
         FW_LAUNCH_CHECK("fw_diag_kernel");
-        prof_end(KC_DIAG, s, (double)kv(t) * kv(t) * kv(t));
+        prof_end(KC_DIAG, q, (double)kv(t) * kv(t) * kv(t));
         return FW_OK;
     }
-    int panels(int t, int h) {
+    int panels(int t, int h, cudaStream_t q = nullptr) {
         if (T < 2) return FW_OK;
+        if (q == nullptr) q = s;
         const int nslab = (int)((kv(t) + kSlab - 1) / kSlab);
-        prof_begin(KC_PANEL, s);
-        fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, s>>>(D, n, ldp, t, nslab, colT + h * kTile * ldp,
+        prof_begin(KC_PANEL, q);
+        fw_panel_kernel<VEC><<<dim3(T - 1, 2), kThreads, kSmemBytes, q>>>(D, n, ldp, t, nslab, colT + h * kTile * ldp,
                                                                          rowP + h * kTile * ldp, 1, skip);
         FW_LAUNCH_CHECK("fw_panel_kernel");
-        prof_end(KC_PANEL, s, 2.0 * (double)(n - kv(t)) * kv(t) * kv(t));
+        prof_end(KC_PANEL, q, 2.0 * (double)(n - kv(t)) * kv(t) * kv(t));
         return FW_OK;
     }
     // Remainder launch over rows x cols with pivots [k_begin, k_end) of the
@@ -267,7 +269,8 @@ struct Blocked {
     // (tiling_gpu; kappa <= 4; needs two panel buffers): after block t's
     // panels, block t's update of block t+1's row and column runs on the
     // caller's stream, the rest of block t's remainder on the side stream
-    // while block t+1 is closed into the other panel buffer.
+    // while block t+1 is closed into the other panel buffer on the
+    // high-priority stream.
     int lookahead() {
         if (int rc = aux_stream_get(s, &aux)) return rc;
         if (int rc = diag(0, 0)) return rc;
@@ -280,10 +283,13 @@ struct Blocked {
             if (int rc = remainder(all_but(t, t + 1), T - 2, only(t + 1), 1, k0, kvt)) return rc;
             FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
             FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+            FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
             if (int rc = remainder(all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, k0, kvt, aux.side)) return rc;
             FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
-            if (int rc = diag(t + 1, h ^ 1)) return rc;
-            if (int rc = panels(t + 1, h ^ 1)) return rc;
+            if (int rc = diag(t + 1, h ^ 1, aux.hi)) return rc;
+            if (int rc = panels(t + 1, h ^ 1, aux.hi)) return rc;
+            FW_CUDA_TRY(cudaEventRecord(aux.hi_done, aux.hi));
+            FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.hi_done, 0));
             FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
         }
         return FW_OK;

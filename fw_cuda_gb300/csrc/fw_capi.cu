@@ -131,9 +131,13 @@ int aux_stream_get(cudaStream_t s, AuxStream* out) {
     std::lock_guard<std::mutex> lk(g_aux_mutex);
     AuxStream& a = g_aux[{dev, s}];
     if (!a.side) {
+        int least = 0, greatest = 0;
+        FW_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         FW_CUDA_TRY(cudaStreamCreateWithFlags(&a.side, cudaStreamNonBlocking));
+        FW_CUDA_TRY(cudaStreamCreateWithPriority(&a.hi, cudaStreamNonBlocking, greatest));
         FW_CUDA_TRY(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
         FW_CUDA_TRY(cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming));
+        FW_CUDA_TRY(cudaEventCreateWithFlags(&a.hi_done, cudaEventDisableTiming));
     }
     *out = a;
     return FW_OK;

@@ -55,14 +55,17 @@ void prof_end(KernelClass kc, cudaStream_t s, double relaxations);
 // error) when allocation fails.
 void* workspace_get(cudaStream_t s, size_t bytes);
 
-// A second, non-blocking stream and a fork / join event pair tied to the
-// caller's (device, stream), created on first use and kept: the look-ahead
-// schedules run the bulk remainder of one pivot block on the side stream while
-// the next block is closed on the caller's stream.
+// Two non-blocking streams and their events tied to the caller's (device,
+// stream), created on first use and kept: the look-ahead schedules run the
+// bulk remainder of one pivot block on `side` while the next block is closed
+// and its panels computed on `hi`, whose highest priority lets its few CTAs
+// take SMs as soon as remainder CTAs retire.
 struct AuxStream {
-    cudaStream_t side = nullptr;
+    cudaStream_t side = nullptr;  // bulk remainder (default priority)
+    cudaStream_t hi = nullptr;    // next block's closure and panels (highest priority)
     cudaEvent_t fork = nullptr;
     cudaEvent_t join = nullptr;
+    cudaEvent_t hi_done = nullptr;
 };
 int aux_stream_get(cudaStream_t s, AuxStream* out);
 

@@ -405,8 +405,8 @@ size_t p16_workspace_bytes(int64_t n) {
 // skip. The sweep looks one pivot block ahead: after block t's panels, the
 // tiles of block t+1's row and column get block t's update on `s`, then the
 // other remainder tiles of block t run on a side stream while block t+1 is
-// closed and its panels computed on `s` (into the other panel buffer); `s`
-// waits for the side stream before block t+1's own remainder.
+// closed and its panels computed on a high-priority stream (into the other
+// panel buffer); `s` waits for both before block t+1's own remainder.
 int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
     static bool attr_done = false;
     if (!attr_done) {
@@ -481,10 +481,13 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
         // the rest of block t's remainder on the side stream ...
         FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
         FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
         if (int rc = remainder(t, all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, aux.side)) return rc;
         FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
-        // ... while block t+1 is closed on the caller's stream
-        if (int rc = close(t + 1, s)) return rc;
+        // ... while block t+1 is closed on the high-priority stream
+        if (int rc = close(t + 1, aux.hi)) return rc;
+        FW_CUDA_TRY(cudaEventRecord(aux.hi_done, aux.hi));
+        FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.hi_done, 0));
         FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
     }
     fw_p16_rmax_kernel<<<grid, 256, 0, s>>>(D16, n, ld, st);
