@@ -136,24 +136,35 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// Phase 3: tiles (I, J), I from `rows`, J from `cols`:
+// Phase 3: tiles (I, J), I from `rows` (nrows of them), J from `cols` (ncols):
 // D[I][J] = min(D[I][J], colT[k][I]^T (x) rowP[k][J]) over workspace pivot
-// rows k in [slab0 * 32, (slab0 + nslab) * 32).
+// rows k in [slab0 * 32, (slab0 + nslab) * 32). Each CTA walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... in row-major order. The launch
+// behind a skip flag is persistent (two CTAs per SM), so when the flag says
+// the packed fast path already produced the result it costs only those CTAs;
+// otherwise there is one CTA per tile, so that the kernels of a higher
+// priority stream can take SMs from it between tiles.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
-    fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, TileSet cols, int slab0, int nslab,
-                        const int* __restrict__ colT, const int* __restrict__ rowP, int one,
+    fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, int nrows, TileSet cols, int ncols,
+                        int slab0, int nslab, const int* __restrict__ colT, const int* __restrict__ rowP, int one,
                         const unsigned* __restrict__ skip) {
     if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int64_t r0 = (int64_t)tile_of(rows, blockIdx.y) * kTile, c0 = (int64_t)tile_of(cols, blockIdx.x) * kTile;
-    int acc[8][8];
-    load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
-    mainloop<kMixA>(
-        acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, (slab0 + s) * kSlab, r0, tid); },
-        [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, (slab0 + s) * kSlab, c0, tid); }, tx, ty, one);
-    store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
+    const int64_t ntiles = (int64_t)nrows * ncols;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t r0 = (int64_t)tile_of(rows, (int)(t / ncols)) * kTile;
+        const int64_t c0 = (int64_t)tile_of(cols, (int)(t % ncols)) * kTile;
+        int acc[8][8];
+        load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
+        mainloop<kMixA>(
+            acc, nslab, smem,
+            [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, (slab0 + s) * kSlab, r0, tid); },
+            [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, (slab0 + s) * kSlab, c0, tid); }, tx, ty, one);
+        store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
+        __syncthreads();  // the next tile's prologue refills the ring
+    }
 }
 
 // Per-pivot sweep. Prime: snapshot row 0 and column 0.
@@ -214,6 +225,7 @@ struct Blocked {
     int* rowP;
     cudaStream_t s;
     const unsigned* skip;
+    int64_t resident_ctas = 304;  // CTAs of the persistent remainder: 2 per SM
     AuxStream aux{};
 
     int64_t p0(int t) const { return (int64_t)t * kTile; }
@@ -248,9 +260,11 @@ struct Blocked {
         if (q == nullptr) q = s;
         const int slab0 = k_begin / kSlab;
         const int nslab = (k_valid + kSlab - 1) / kSlab;
+        const int64_t ntiles = (int64_t)nrows * ncols;
+        const unsigned grid = (unsigned)((skip && ntiles > resident_ctas) ? resident_ctas : ntiles);
         prof_begin(KC_REMAINDER, q);
-        fw_remainder_kernel<VEC><<<dim3(ncols, nrows), kThreads, kSmemBytes, q>>>(D, n, ldp, rows, cols, slab0, nslab,
-                                                                                 colT, rowP, 1, skip);
+        fw_remainder_kernel<VEC><<<grid, kThreads, kSmemBytes, q>>>(D, n, ldp, rows, nrows, cols, ncols, slab0, nslab,
+                                                                    colT, rowP, 1, skip);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
         prof_end(KC_REMAINDER, q, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
         return FW_OK;
@@ -340,6 +354,12 @@ int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahea
     }
     Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip};
     b.ldp = (int64_t)b.T * kTile;
+    {
+        int dev = 0, sms = 0;
+        FW_CUDA_TRY(cudaGetDevice(&dev));
+        FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        b.resident_ctas = 2 * (int64_t)(sms > 0 ? sms : 152);
+    }
     if (blocks_per_pass == 1 && lookahead && b.T > 2) return b.lookahead();
     for (int t = 0; t < b.T;) {
         if (blocks_per_pass == 2 && t + 1 < b.T) {

@@ -225,7 +225,10 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
             std::lock_guard<std::mutex> lk(g_ws_mutex);
             g_auto_done[{dev, s}] = done;
         }
-        return blocked_solve(d_D, n, blocks, d_workspace, blocked, s, done);
+        // The int32 fallback behind the flag runs the two-block schedule on
+        // one stream: its remainder launches are persistent, so that they
+        // cost little when the packed result is taken.
+        return blocked_solve(d_D, n, 2, d_workspace, blocked, s, done);
     }
     return blocked_solve(d_D, n, blocks, d_workspace, workspace_bytes, s);
 }
