@@ -30,6 +30,7 @@ FW_ERR_CUDA = 2
 FW_ERR_NO_MEMORY = 3
 FW_ERR_TIMEOUT = 4
 FW_ERR_NOT_BUILT = 5
+FW_ERR_INTERNAL = 6
 
 VARIANT_BASELINE = 0
 VARIANT_TILING = 1
@@ -53,6 +54,10 @@ EXPORTED_SYMBOLS = (
     "fw_path_length_i32",
     "fw_dense_from_csr_i32",
     "fw_negative_cycle_i32",
+    "fw_apsp_i32_host",
+    "fw_generate_graph_device_i32",
+    "fw_mt19937_outputs",
+    "fw_host_solve_device_bytes",
     "fw_batch_pack_offsets",
     "fw_batch_plan_create",
     "fw_batch_plan_autotune",
@@ -123,6 +128,15 @@ def lib():
     L.fw_dense_from_csr_i32.restype = c_int
     L.fw_negative_cycle_i32.argtypes = [vp, i64, i64, vp, vp]
     L.fw_negative_cycle_i32.restype = c_int
+    L.fw_generate_graph_device_i32.argtypes = [vp, i64, ctypes.c_double, ctypes.c_uint32, ctypes.c_int32,
+                                               ctypes.c_int32, vp]
+    L.fw_generate_graph_device_i32.restype = c_int
+    L.fw_mt19937_outputs.argtypes = [ctypes.c_uint32, ctypes.c_uint64, i64, vp]
+    L.fw_mt19937_outputs.restype = c_int
+    L.fw_apsp_i32_host.argtypes = [vp, i64, i64, i64, vp]
+    L.fw_apsp_i32_host.restype = c_int
+    L.fw_host_solve_device_bytes.argtypes = [i64, i64, i64]
+    L.fw_host_solve_device_bytes.restype = ctypes.c_size_t
     L.fw_measure_relax_peak_packed.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak_packed.restype = c_int
     L.fw_apsp_auto_report.argtypes = [vp, ctypes.POINTER(c_int)]
@@ -201,6 +215,19 @@ def generate_graph(n: int, density: float, seed: int, wmin: int = 0, wmax: int =
     return out
 
 
+def generate_graph_device(d_D, n: int, density: float, seed: int, wmin: int = 0, wmax: int = MAX_EDGE_WEIGHT,
+                          stream=None) -> None:
+    """generate_graph's matrix, value for value, generated on the device into d_D."""
+    _check(lib().fw_generate_graph_device_i32(_ptr(d_D), n, float(density), seed, wmin, wmax, _stream(stream)))
+
+
+def mt19937_outputs(seed: int, skip: int, count: int) -> np.ndarray:
+    """Host: `count` std::mt19937(seed) outputs after the first `skip`, by polynomial jump-ahead."""
+    out = np.empty(count, dtype=np.uint32)
+    _check(lib().fw_mt19937_outputs(seed, skip, count, out.ctypes.data))
+    return out
+
+
 def version() -> str:
     return lib().fw_version().decode()
 
@@ -264,6 +291,27 @@ def dense_from_csr(d_rowptr, d_col, d_w, n: int, d_D, d_bad=None, stream=None) -
 def negative_cycle_flags(d_D, n: int, batch: int, d_flags, stream=None) -> None:
     """d_flags[b] = 1 if graph b has a negative diagonal entry (hasNegativeCycle)."""
     _check(lib().fw_negative_cycle_i32(_ptr(d_D), n, batch, _ptr(d_flags), _stream(stream)))
+
+
+def apsp_i32_host(h_D, n: int, pass_width: int = 0, stripe_rows: int = 0, stream=None) -> None:
+    """In-place APSP of an n x n int32 matrix held in HOST memory (a C-contiguous
+    numpy array or CPU tensor), streamed through the device in row stripes;
+    returns when h_D holds the result."""
+    if hasattr(h_D, "data_ptr"):
+        if h_D.is_cuda or not h_D.is_contiguous():
+            raise ValueError("expected a contiguous CPU tensor")
+        addr = h_D.data_ptr()
+    elif isinstance(h_D, np.ndarray):
+        if h_D.dtype != np.int32 or not h_D.flags.c_contiguous or not h_D.flags.writeable:
+            raise ValueError("expected a writeable C-contiguous int32 array")
+        addr = h_D.ctypes.data
+    else:
+        raise TypeError(f"cannot take a host address of {type(h_D)!r}")
+    _check(lib().fw_apsp_i32_host(addr, n, pass_width, stripe_rows, _stream(stream)))
+
+
+def host_solve_device_bytes(n: int, pass_width: int, stripe_rows: int) -> int:
+    return int(lib().fw_host_solve_device_bytes(n, pass_width, stripe_rows))
 
 
 # ----------------------------------------------------------------- batched APSP

@@ -49,7 +49,7 @@ ProfState g_prof;
 const char* const kClassNames[KC_COUNT] = {"fw_diag",          "fw_panel",        "fw_remainder",
                                            "fw_pivot_step",    "fw_batched",      "fw_forward_f32",
                                            "fw_backward_f32",  "fw_p16_diag",     "fw_p16_panel",
-                                           "fw_p16_remainder", "fw_paths_i32"};
+                                           "fw_p16_remainder", "fw_paths_i32",    "fw_ooc_update"};
 
 cudaEvent_t prof_event() {
     if (g_prof.next == g_prof.pool.size()) {

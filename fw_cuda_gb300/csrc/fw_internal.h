@@ -42,6 +42,7 @@ enum KernelClass {
     KC_P16_PANEL,
     KC_P16_REMAINDER,
     KC_PATHS_I32,
+    KC_OOC_UPDATE,
     KC_COUNT
 };
 
@@ -96,6 +97,11 @@ int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStrea
 int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s);
 // int32 sweep that also records next hops (same kernels as the fp32 form).
 int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
+
+// Out-of-core sweep over a host-resident matrix (fw_ooc.cu); W and H are
+// validated multiples of 128.
+size_t ooc_device_bytes(int64_t n, int64_t W, int64_t H);
+int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s);
 
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);

@@ -38,7 +38,8 @@ typedef enum fw_status {
     FW_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
     FW_ERR_NO_MEMORY = 3,        /* workspace allocation failed */
     FW_ERR_TIMEOUT = 4,          /* a bounded device-side wait gave up */
-    FW_ERR_NOT_BUILT = 5         /* device code for this GPU is absent */
+    FW_ERR_NOT_BUILT = 5,        /* device code for this GPU is absent */
+    FW_ERR_INTERNAL = 6          /* an internal consistency check failed */
 } fw_status;
 
 /* Which of the reference's three GPU algorithms a call stands in for
@@ -88,6 +89,26 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
  * by the caller. The first call on each device looks up the array's device
  * address (cudaGetSymbolAddress); make it before any stream capture. */
 int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
+
+/* ---------------------------------------------------------------- out-of-core */
+
+/* Solves an n x n int32 row-major matrix that stays in HOST memory, in place,
+ * for matrices larger than the device's memory (the reference caps n at
+ * MAX_N = 32769, include/constants.h:5, and copies the whole matrix to the
+ * device, src/gpu_memory.cu:13-16). Each pass of `pass_width` pivots
+ * (a multiple of 128; 0 = 2048) streams the matrix through the device in row
+ * stripes of `stripe_rows` rows (a multiple of 128; 0 = chosen from the free
+ * device memory), so a pass moves 8 n^2 bytes for pass_width * n^2
+ * relaxations. The result is bit-identical to fw_apsp_i32. Page-locked host
+ * memory gives asynchronous copies; pageable memory is registered for the
+ * duration of the call when possible. Allocates its device buffers per call
+ * (fw_host_solve_device_bytes) and returns when h_D holds the result; work is
+ * enqueued on `stream` and two streams of its own. */
+int fw_apsp_i32_host(int32_t* h_D, int64_t n, int64_t pass_width, int64_t stripe_rows, fw_stream_t stream);
+
+/* Device bytes fw_apsp_i32_host allocates for these arguments (0 for invalid
+ * ones; stripe_rows must be given, not 0). */
+size_t fw_host_solve_device_bytes(int64_t n, int64_t pass_width, int64_t stripe_rows);
 
 /* ---------------------------------------------------------------- path reconstruction */
 
@@ -184,6 +205,22 @@ int fw_backward(const float* d_dLdD, const int32_t* d_nh, float* d_dLdW, int64_t
  * generateAlignedGraph1D byte for byte under the same libstdc++. */
 int fw_generate_graph_i32(int32_t* h_out, int64_t n, double density, uint32_t seed,
                           int32_t wmin, int32_t wmax);
+
+/* fw_generate_graph_i32's matrix, value for value, generated on the device
+ * into d_D (n*n int32): the MT19937 word stream is produced in parallel
+ * chunks whose starting states come from polynomial jump-ahead, and the
+ * variable-length draws (two words per pair, one more per edge and per
+ * rejection of the weight draw) are parsed in parallel. Replaces the host
+ * generation of src/graph_generator.cpp:7-46 and the n*n host-to-device
+ * copy of src/gpu_memory.cu:13-16. Allocates ~4 bytes per generator word
+ * (about 2 + density words per pair) on `stream` and returns when d_D is
+ * written. */
+int fw_generate_graph_device_i32(int32_t* d_D, int64_t n, double density, uint32_t seed,
+                                 int32_t wmin, int32_t wmax, fw_stream_t stream);
+
+/* Host: `count` outputs of std::mt19937(seed) starting after the first
+ * `skip` outputs, computed by the same polynomial jump-ahead (no device). */
+int fw_mt19937_outputs(uint32_t seed, uint64_t skip, int64_t count, uint32_t* h_out);
 
 /* Message of the last failure on this host thread ("" if none). */
 const char* fw_last_error_string(void);

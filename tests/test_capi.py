@@ -8,6 +8,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from conftest import ROOT, sha, load_json
 
@@ -60,6 +61,32 @@ def test_bad_arguments_fail_before_any_device_work(fw):
     assert L.fw_apsp_i32_ws(fake, 1000, 32, 4, 2, fake + 16, need, None) == fw.FW_ERR_INVALID_ARGUMENT
     # the per-pivot sweep puts one row per grid row
     assert L.fw_apsp_i32_ws(fake, 70000, 0, 0, 0, fake, 1 << 40, None) == fw.FW_ERR_INVALID_ARGUMENT
+
+
+def test_host_solve_arguments(fw):
+    L = fw.lib()
+    fake = 0x7F0000000000  # never dereferenced: every check below fails first
+    assert L.fw_apsp_i32_host(None, 16, 0, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"NULL" in L.fw_last_error_string()
+    assert L.fw_apsp_i32_host(fake, 0, 0, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert L.fw_apsp_i32_host(fake, 3_000_000, 0, 0, None) == fw.FW_ERR_INVALID_ARGUMENT
+    for bad_w in (-128, 100, 64):
+        assert L.fw_apsp_i32_host(fake, 1000, bad_w, 128, None) == fw.FW_ERR_INVALID_ARGUMENT
+        assert b"pass_width" in L.fw_last_error_string()
+    for bad_h in (-128, 200):
+        assert L.fw_apsp_i32_host(fake, 1000, 256, bad_h, None) == fw.FW_ERR_INVALID_ARGUMENT
+        assert b"stripe_rows" in L.fw_last_error_string()
+    with pytest.raises(ValueError):
+        fw.apsp_i32_host(np.zeros((4, 4), dtype=np.int64), 4)
+    # device bytes: four W x ldp panels, the n x W column stripe, Dg, two
+    # padded copies of Dg*, three H x n stripes
+    n, W, H = 1000, 256, 384
+    ldp = 1024
+    want = 4 * (4 * W * ldp + n * W + W * W + 2 * W * W + 3 * H * n)
+    assert fw.host_solve_device_bytes(n, W, H) == want
+    assert fw.host_solve_device_bytes(100, 0, 128) == 4 * (4 * 128 * 128 + 100 * 128 + 128 * 128 + 2 * 128 * 128
+                                                           + 3 * 128 * 100)
+    assert fw.host_solve_device_bytes(n, W, 0) == 0
 
 
 def test_workspace_sizes(fw):
