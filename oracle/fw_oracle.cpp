@@ -19,6 +19,8 @@
 //     optionally with the i-loop split over host threads (one barrier per
 //     pivot). Used to time bounded samples of a large solve.
 //   * oracle_has_negative_cycle: src/utils.cpp:5-12.
+//   * oracle_mt19937_outputs: std::mt19937 outputs after a discard, the
+//     engine the generator draws from.
 // Added checkers with no reference counterpart:
 //   * oracle_sssp_dense: dense Dijkstra from one source on the same INF
 //     convention (exact for non-negative weights); checks sampled rows of a
@@ -151,6 +153,15 @@ void oracle_fw_i32_pivots(int32_t* D, int64_t n, int64_t k0, int64_t k1, int thr
     for (int t = 1; t < threads; ++t) pool.emplace_back(worker, t);
     worker(0);
     for (auto& th : pool) th.join();
+}
+
+// `count` outputs of std::mt19937(seed) after discarding the first `skip`
+// (the engine of src/graph_generator.cpp:18), straight from the standard
+// library: the checker for the jump-ahead of the device generator.
+void oracle_mt19937_outputs(uint32_t seed, uint64_t skip, int64_t count, uint32_t* out) {
+    std::mt19937 gen(seed);
+    gen.discard(skip);
+    for (int64_t i = 0; i < count; ++i) out[i] = static_cast<uint32_t>(gen());
 }
 
 // src/utils.cpp:5-12.

@@ -69,6 +69,9 @@ def lib():
         L.oracle_fw_f32_nexthop.restype = None
         L.oracle_fw_backward.argtypes = [_f64p, _i32p, _i64, _f64p]
         L.oracle_fw_backward.restype = _i64
+        L.oracle_mt19937_outputs.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _i64,
+                                             np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")]
+        L.oracle_mt19937_outputs.restype = None
         _lib = L
     return _lib
 
@@ -93,6 +96,12 @@ def fw_i32_pivots(D: np.ndarray, k0: int, k1: int, threads: int = 1) -> None:
     """Pivots [k0, k1) of the sweep, in place."""
     assert D.dtype == np.int32 and D.flags.c_contiguous
     lib().oracle_fw_i32_pivots(D, D.shape[0], k0, k1, threads)
+
+
+def mt19937_outputs(seed: int, skip: int, count: int) -> np.ndarray:
+    out = np.empty(count, dtype=np.uint32)
+    lib().oracle_mt19937_outputs(seed, skip, count, out)
+    return out
 
 
 def has_negative_cycle(D: np.ndarray) -> bool:

@@ -136,3 +136,14 @@ def test_reference_library_agrees(oracle):
         b = a.copy()
         R.ref_fw_baseline_cpu(b, n)
         assert np.array_equal(b, oracle.fw_i32(a))
+
+
+def test_mt19937_jump_ahead_matches_std(fw, oracle):
+    """The device generator's starting states come from polynomial jump-ahead
+    (host side of fw_generate_graph_device_i32); its outputs after a skip
+    equal std::mt19937 after discard(skip)."""
+    for seed, skip in [(5489, 0), (42, 1), (42, 623), (42, 624), (7, 625), (123, 2**25),
+                       (99, 3 * 2**25 + 17), (7, 2**28 + 12345)]:
+        count = 1500
+        assert np.array_equal(fw.mt19937_outputs(seed, skip, count),
+                              oracle.mt19937_outputs(seed, skip, count)), (seed, skip)
