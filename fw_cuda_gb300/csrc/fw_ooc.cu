@@ -11,13 +11,14 @@
 //   3. R2 = min(R, Dg* (x) R) and CT2 = min(CT, Dg*^T (x) CT) — the row and
 //      column panels of the pass, as min-plus products (Dg* is closed, so
 //      neither depends on a k order).
-//   4. Every row stripe D[I][:] goes host -> device, becomes
-//      min(D[I][:], CT2[:, I]^T (x) R2) and goes back. The update is applied
-//      to the stripe's rows and columns inside P too: with no negative cycle
-//      it leaves the panels (R2 on the rows of P, CT2 transposed on the
-//      columns of P) and Dg* on the diagonal block, exactly the values of the
-//      in-core sweep, so the result is bit-identical to it and to the k-i-j
-//      sweep of src/fw_baseline_cpu.cpp:6-15.
+//   4. Every row stripe D[I][:] goes host -> device; its tiles outside the
+//      rows and columns of P become min(D[I][J], CT2[:, I]^T (x) R2[:, J]),
+//      its columns in P take the column panel (CT2 transposed back) and its
+//      rows in P the row panel R2; then it goes back. These are the values
+//      of the in-core sweep after the same pivots, so the result is
+//      bit-identical to it and to the k-i-j sweep of
+//      src/fw_baseline_cpu.cpp:6-15, and the relaxations done are n^3 plus
+//      the W^3 of each diagonal closure.
 // Three stripe buffers rotate over a copy-in stream, the caller's stream
 // (compute) and a copy-out stream, so the host transfers of one stripe
 // overlap the update of the next. A pass moves 8 n^2 bytes over the host link
@@ -104,21 +105,29 @@ __device__ __forceinline__ void ooc_store_acc(const int (&acc)[8][8], int* __res
     }
 }
 
+// Tile rows [x0, x1) (or columns) left out of an update.
+struct TileGap {
+    int64_t x0, x1;
+};
+__device__ __forceinline__ int64_t skip_gap(int64_t idx, const TileGap& g) { return idx < g.x0 ? idx : idx + (g.x1 - g.x0); }
+
 // C[i][j] = min(C[i][j], min_k A[k][i] + B[k][j]) for i < M, j < N and
-// k < 32 * nslab. A and B are k-major with leading dimensions that are
-// multiples of 4 and cover whole 128-wide tiles (INF where there is no
-// value), as are their 32-row slabs. Each CTA walks the tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ... The main loop is the in-core remainder's.
+// k < 32 * nslab, over the 128 x 128 tiles outside the row gap and the column
+// gap. A and B are k-major with leading dimensions that are multiples of 4
+// and cover whole 128-wide tiles (INF where there is no value), as are their
+// 32-row slabs. Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x,
+// ... The main loop is the in-core remainder's.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_ooc_update_kernel(int* __restrict__ C, int64_t ldc, int64_t M, int64_t N, const int* __restrict__ A,
-                         int64_t lda, const int* __restrict__ B, int64_t ldb, int nslab, int one) {
+                         int64_t lda, const int* __restrict__ B, int64_t ldb, int nslab, TileGap rgap, TileGap cgap,
+                         int one) {
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int64_t tn = (N + kTile - 1) / kTile;
-    const int64_t ntiles = ((M + kTile - 1) / kTile) * tn;
+    const int64_t tn = (N + kTile - 1) / kTile - (cgap.x1 - cgap.x0);
+    const int64_t ntiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * tn;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t r0 = (t / tn) * kTile, c0 = (t % tn) * kTile;
+        const int64_t r0 = skip_gap(t / tn, rgap) * kTile, c0 = skip_gap(t % tn, cgap) * kTile;
         int acc[8][8];
         ooc_load_acc<VEC>(acc, C, ldc, M, N, r0, c0, tx, ty);
         mainloop<kMixA>(
@@ -183,19 +192,24 @@ int transpose(const int* src, int64_t lds, int* dst, int64_t ldd, int64_t rows, 
 }
 
 int update(int* C, int64_t ldc, int64_t M, int64_t N, const int* A, int64_t lda, const int* B, int64_t ldb,
-           int64_t kvalid, int64_t resident, cudaStream_t s) {
-    const int64_t tiles = ((M + kTile - 1) / kTile) * ((N + kTile - 1) / kTile);
+           int64_t kvalid, int64_t resident, cudaStream_t s, TileGap rgap = {0, 0}, TileGap cgap = {0, 0}) {
+    const int64_t tiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * ((N + kTile - 1) / kTile - (cgap.x1 - cgap.x0));
+    if (tiles <= 0) return FW_OK;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, resident);
     const int nslab = (int)((kvalid + kSlab - 1) / kSlab);
     // 16-byte accesses need aligned rows and whole vectors inside [0, N).
     const bool vec = (ldc % 4) == 0 && (N % 4) == 0 && (reinterpret_cast<uintptr_t>(C) & 15u) == 0;
     prof_begin(KC_OOC_UPDATE, s);
     if (vec)
-        fw_ooc_update_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, 1);
+        fw_ooc_update_kernel<true>
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, rgap, cgap, 1);
     else
-        fw_ooc_update_kernel<false><<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, 1);
+        fw_ooc_update_kernel<false>
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, rgap, cgap, 1);
     FW_LAUNCH_CHECK("fw_ooc_update_kernel");
-    prof_end(KC_OOC_UPDATE, s, (double)M * (double)N * (double)kvalid);
+    const double rows = (double)M - std::min<double>((double)M, (double)(rgap.x1 - rgap.x0) * kTile);
+    const double cols = (double)N - std::min<double>((double)N, (double)(cgap.x1 - cgap.x0) * kTile);
+    prof_end(KC_OOC_UPDATE, s, std::max(rows, 0.0) * std::max(cols, 0.0) * (double)kvalid);
     return FW_OK;
 }
 
@@ -311,7 +325,19 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
             FW_CUDA_TRY(cudaMemcpyAsync(st.buf[b], h_D + r0 * n, sb, cudaMemcpyHostToDevice, st.in));
             FW_CUDA_TRY(cudaEventRecord(st.ev_in[b], st.in));
             FW_CUDA_TRY(cudaStreamWaitEvent(s, st.ev_in[b], 0));
-            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, st.R2, ldp, w, resident, s)) return rc;
+            // tiles outside P's rows and columns: the min-plus update
+            const int64_t pr0 = std::max(p0, r0), pr1 = std::min(p0 + w, r0 + h);  // P rows in the stripe
+            const TileGap rgap = pr0 < pr1 ? TileGap{(pr0 - r0) / kTile, (pr1 - r0 + kTile - 1) / kTile} : TileGap{0, 0};
+            const TileGap cgap{p0 / kTile, (p0 + w + kTile - 1) / kTile};
+            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, st.R2, ldp, w, resident, s, rgap, cgap))
+                return rc;
+            // columns of P: the column panel, transposed back
+            if (int rc = transpose(st.CT2 + r0, ldp, st.buf[b] + p0, n, w, h, s)) return rc;
+            // rows of P: the row panel
+            if (pr0 < pr1)
+                FW_CUDA_TRY(cudaMemcpy2DAsync(st.buf[b] + (pr0 - r0) * n, n * sizeof(int), st.R2 + (pr0 - p0) * ldp,
+                                              ldp * sizeof(int), n * sizeof(int), pr1 - pr0, cudaMemcpyDeviceToDevice,
+                                              s));
             FW_CUDA_TRY(cudaEventRecord(st.ev_comp[b], s));
             FW_CUDA_TRY(cudaStreamWaitEvent(st.out, st.ev_comp[b], 0));
             FW_CUDA_TRY(cudaMemcpyAsync(h_D + r0 * n, st.buf[b], sb, cudaMemcpyDeviceToHost, st.out));
@@ -369,6 +395,9 @@ int fw_apsp_i32_host(int32_t* h_D, int64_t n, int64_t pass_width, int64_t stripe
         double budget = ((double)free_b - fixed - (double)(1ull << 30)) / 2.0;
         budget = std::min(budget, 12.0 * (double)(1ull << 30));
         H = (int64_t)(budget / (3.0 * 4.0 * (double)n)) / kTile * kTile;
+        // at least 8 stripes per pass, so the copies of one stripe hide
+        // behind the update of the others
+        H = std::min(H, round_up((n + 7) / 8, kTile));
         if (H < kTile) H = kTile;
     } else if (H < kTile || H % kTile != 0) {
         return set_error(FW_ERR_INVALID_ARGUMENT,
