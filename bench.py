@@ -327,22 +327,24 @@ def run_ours(args) -> None:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     if used_packed:
-        roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, peak_packed,
+        roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, 512, peak_packed,
                                "measured live: register-only packed 16-bit DPX add-min kernel "
-                               "(fw_measure_relax_peak_packed)", hbm_peak, "hbm_gbs" in peaks)
+                               "(fw_measure_relax_peak_packed)", hbm_peak, "hbm_gbs" in peaks,
+                               traffic_at_16384=532.27e6 + 445.96e6)
         if roofline:
             roofline["int32_dpx_only_peak"] = peak_dpx
     else:
-        roofline = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 128, 4, peak_mixed,
+        pair = variant == VARIANTS["multi_layer_tiling_gpu"] and args.kappa > 4
+        # bulk launch: all tiles outside two pivot blocks (the two-block pass,
+        # or the look-ahead of the one-block pass)
+        roofline = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 256 if pair else 128, 4,
+                               256, peak_mixed,
                                "measured live: register-only relaxation kernels (fw_measure_relax_peak), "
-                               "best instruction mix", hbm_peak, "hbm_gbs" in peaks)
+                               "best instruction mix", hbm_peak, "hbm_gbs" in peaks,
+                               traffic_at_16384=(1.11e9 + 983.25e6) if pair else None)
         if roofline:
             roofline["dpx_only_peak"] = peak_dpx
             roofline["frac_of_dpx_only"] = roofline["achieved"] / peak_dpx
-            if args.kappa <= 4:
-                # ncu (profiles/fw_remainder_n8192.md): 468.4 MB of DRAM traffic per remainder
-                # launch at n = 8192 (63^2 tiles); traffic scales with the tiles a launch touches.
-                roofline["traffic"] = 468.4e6 * ((n - 128) / 8064.0) ** 2
     int32_path = None
     if variant == VARIANTS["auto"] and not args.no_int32:
         int32_path = time_variant(F, torch, stream, work, pristine, n, args.kappa, VARIANTS["multi_layer_tiling_gpu"],
@@ -391,23 +393,37 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
-def roofline_of(stats, kernel, n, block, bytes_per_value, peak, peak_source, hbm_peak, hbm_measured):
-    """Roofline of the dominant kernel from its event-timed launches."""
+def roofline_of(stats, kernel, n, pivots, bytes_per_value, gap, peak, peak_source, hbm_peak, hbm_measured,
+                traffic_at_16384=None):
+    """Roofline of the dominant kernel from its event-timed launches.
+
+    Work: relaxations. Algorithmic bytes: a launch with K pivots reads and
+    writes each of its tiles once, so its tile bytes are relaxations * 2 *
+    bytes_per_value / K (the panels it streams, K * n values, are left out:
+    under 2 % at n = 32768). The bulk launch of a pass covers (n - gap)^2
+    entries; `traffic_at_16384` is ncu's dram__bytes_read.sum +
+    dram__bytes_write.sum for that launch at n = 16384 (one pass, the matrix
+    well above L2), scaled by the entries a launch touches."""
     if not stats or not stats["launches"]:
         return None
     secs = stats["total_ms"] / 1e3
     achieved = stats["relaxations"] / secs
-    # algorithmic bytes of one remainder launch: its tiles read + written once,
-    # plus the two `block`-wide panels it streams (n' = n - block)
-    nr = n - block
-    bytes_per_launch = 2.0 * bytes_per_value * nr * nr + 2.0 * 4 * block * nr
-    hbm_gbs = bytes_per_launch * stats["launches"] / secs / 1e9
-    return {"kernel": kernel, "bound": "int_issue", "achieved": achieved, "peak": peak, "unit": UNIT,
-            "frac": achieved / peak, "peak_source": peak_source, "traffic": None,
-            "avg_launch_ms": stats["total_ms"] / stats["launches"],
-            "relax_per_launch": stats["relaxations"] / stats["launches"],
-            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm_measured else "fallback"}}
+    tile_bytes = stats["relaxations"] * 2.0 * bytes_per_value / pivots
+    hbm_gbs = tile_bytes / secs / 1e9
+    bulk_bytes = 2.0 * bytes_per_value * (n - gap) ** 2
+    out = {"kernel": kernel, "bound": "int_issue", "achieved": achieved, "peak": peak, "unit": UNIT,
+           "frac": achieved / peak, "peak_source": peak_source, "traffic": None,
+           "avg_launch_ms": stats["total_ms"] / stats["launches"],
+           "relax_per_launch": stats["relaxations"] / stats["launches"],
+           "bulk_launch": {"pivots": pivots, "entries": (n - gap) ** 2, "algorithmic_bytes": bulk_bytes},
+           "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm_measured else "fallback"}}
+    if traffic_at_16384:
+        out["traffic"] = traffic_at_16384 * ((n - gap) / (16384.0 - gap)) ** 2
+        out["traffic_unit"] = "bytes per bulk launch"
+        out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk launch at "
+                                 "n = 16384, scaled by (n - %d)^2" % gap)
+    return out
 
 
 def time_variant(F, torch, stream, work, pristine, n, kappa, variant, steps, world, relax) -> dict:
