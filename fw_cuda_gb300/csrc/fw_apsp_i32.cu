@@ -144,18 +144,31 @@ __global__ void __launch_bounds__(kThreads, 2)
 // the packed fast path already produced the result it costs only those CTAs;
 // otherwise there is one CTA per tile, so that the kernels of a higher
 // priority stream can take SMs from it between tiles.
+// With cross >= 0 the tiles are instead block `cross`'s update of block
+// u = cross + 1's row and column: tiles [0, nrows - 1) are (u, J), J != cross,
+// the next nrows - 2 are (I, u), I != cross, u (nrows = T, ncols = 2T - 3).
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, int nrows, TileSet cols, int ncols,
                         int slab0, int nslab, const int* __restrict__ colT, const int* __restrict__ rowP, int one,
-                        const unsigned* __restrict__ skip) {
+                        const unsigned* __restrict__ skip, int cross) {
     if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int64_t ntiles = (int64_t)nrows * ncols;
+    const int64_t ntiles = cross >= 0 ? (int64_t)ncols : (int64_t)nrows * ncols;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t r0 = (int64_t)tile_of(rows, (int)(t / ncols)) * kTile;
-        const int64_t c0 = (int64_t)tile_of(cols, (int)(t % ncols)) * kTile;
+        int I, J;
+        if (cross < 0) {
+            I = tile_of(rows, (int)(t / ncols));
+            J = tile_of(cols, (int)(t % ncols));
+        } else if (t < nrows - 1) {
+            I = cross + 1;
+            J = tile_of(all_but(cross), (int)t);
+        } else {
+            I = tile_of(all_but(cross, cross + 1), (int)t - (nrows - 1));
+            J = cross + 1;
+        }
+        const int64_t r0 = (int64_t)I * kTile, c0 = (int64_t)J * kTile;
         int acc[8][8];
         load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
         mainloop<kMixA>(
@@ -255,19 +268,28 @@ struct Blocked {
     // Remainder launch over rows x cols with pivots [k_begin, k_end) of the
     // workspace (k_end - k_begin valid pivots; slabs rounded up).
     int remainder(TileSet rows, int nrows, TileSet cols, int ncols, int k_begin, int k_valid,
-                  cudaStream_t q = nullptr) {
+                  cudaStream_t q = nullptr, int cross = -1) {
         if (nrows <= 0 || ncols <= 0 || k_valid <= 0) return FW_OK;
         if (q == nullptr) q = s;
         const int slab0 = k_begin / kSlab;
         const int nslab = (k_valid + kSlab - 1) / kSlab;
-        const int64_t ntiles = (int64_t)nrows * ncols;
+        const int64_t ntiles = cross >= 0 ? (int64_t)ncols : (int64_t)nrows * ncols;
         const unsigned grid = (unsigned)((skip && ntiles > resident_ctas) ? resident_ctas : ntiles);
         prof_begin(KC_REMAINDER, q);
         fw_remainder_kernel<VEC><<<grid, kThreads, kSmemBytes, q>>>(D, n, ldp, rows, nrows, cols, ncols, slab0, nslab,
-                                                                    colT, rowP, 1, skip);
+                                                                    colT, rowP, 1, skip, cross);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
-        prof_end(KC_REMAINDER, q, relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid);
+        const double relax = cross >= 0
+                                 ? ((double)kv(cross + 1) * (double)(n - kv(cross)) +
+                                    (double)(n - kv(cross) - kv(cross + 1)) * (double)kv(cross + 1)) *
+                                       (double)k_valid
+                                 : relax_of(rows, nrows) * relax_of(cols, ncols) * (double)k_valid;
+        prof_end(KC_REMAINDER, q, relax);
         return FW_OK;
+    }
+    // Block t's update of block t + 1's row and column, one launch.
+    int cross_update(int t, int k_begin, int k_valid, cudaStream_t q) {
+        return remainder(TileSet{-1, -1, -1}, T, TileSet{-1, -1, -1}, 2 * T - 3, k_begin, k_valid, q, t);
     }
     // Number of matrix rows (or columns) the tile set covers.
     double relax_of(const TileSet& ts, int count) const {
@@ -280,32 +302,41 @@ struct Blocked {
     }
 
     // One 128-wide pivot block per remainder pass with a one-block look-ahead
-    // (tiling_gpu; kappa <= 4; needs two panel buffers): after block t's
-    // panels, block t's update of block t+1's row and column runs on the
-    // caller's stream, the rest of block t's remainder on the side stream
-    // while block t+1 is closed into the other panel buffer on the
-    // high-priority stream.
+    // (tiling_gpu; kappa <= 4; needs two panel buffers). The high-priority
+    // stream carries the chain every later block waits for — block t's update
+    // of block t+1's row and column (one launch), then block t+1's closure and
+    // panels into the other buffer — while the side stream runs block t's bulk
+    // remainder (every tile outside both blocks) concurrently. The chain for
+    // block t+1 starts once block t-1's bulk is done (its tiles, and the
+    // panel buffer block t+1 reuses).
     int lookahead() {
         if (int rc = aux_stream_get(s, &aux)) return rc;
-        if (int rc = diag(0, 0)) return rc;
-        if (int rc = panels(0, 0)) return rc;
+        FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+        if (int rc = diag(0, 0, aux.hi)) return rc;
+        if (int rc = panels(0, 0, aux.hi)) return rc;
+        FW_CUDA_TRY(cudaEventRecord(aux.panels[0], aux.hi));
         for (int t = 0; t < T; ++t) {
             const int h = t & 1;
             const int k0 = h * kTile, kvt = (int)kv(t);
-            if (t + 1 >= T) return remainder(all_but(t), T - 1, all_but(t), T - 1, k0, kvt);
-            if (int rc = remainder(only(t + 1), 1, all_but(t), T - 1, k0, kvt)) return rc;
-            if (int rc = remainder(all_but(t, t + 1), T - 2, only(t + 1), 1, k0, kvt)) return rc;
-            FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
-            FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
-            FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
-            if (int rc = remainder(all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, k0, kvt, aux.side)) return rc;
-            FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
-            if (int rc = diag(t + 1, h ^ 1, aux.hi)) return rc;
-            if (int rc = panels(t + 1, h ^ 1, aux.hi)) return rc;
-            FW_CUDA_TRY(cudaEventRecord(aux.hi_done, aux.hi));
-            FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.hi_done, 0));
-            FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
+            if (t + 1 < T) {
+                if (t >= 1) FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.bulk[(t - 1) & 1], 0));
+                if (int rc = cross_update(t, k0, kvt, aux.hi)) return rc;
+                if (int rc = diag(t + 1, h ^ 1, aux.hi)) return rc;
+                if (int rc = panels(t + 1, h ^ 1, aux.hi)) return rc;
+                FW_CUDA_TRY(cudaEventRecord(aux.panels[(t + 1) & 1], aux.hi));
+            }
+            FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.panels[h], 0));
+            if (t + 1 < T) {
+                if (int rc = remainder(all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, k0, kvt, aux.side)) return rc;
+            } else {
+                if (int rc = remainder(all_but(t), T - 1, all_but(t), T - 1, k0, kvt, aux.side)) return rc;
+            }
+            FW_CUDA_TRY(cudaEventRecord(aux.bulk[h], aux.side));
         }
+        // the side stream's last launch follows every launch of the chain
+        FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.bulk[(T - 1) & 1], 0));
         return FW_OK;
     }
 

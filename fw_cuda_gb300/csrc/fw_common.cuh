@@ -164,7 +164,7 @@ __device__ __forceinline__ int tile_of(const TileSet& s, int idx) {
     return idx;
 }
 
-inline TileSet all_but(int a, int b = -1) {
+__host__ __device__ inline TileSet all_but(int a, int b = -1) {
     if (b >= 0 && b < a) {
         const int t = a;
         a = b;
@@ -176,7 +176,7 @@ inline TileSet all_but(int a, int b = -1) {
     }
     return TileSet{-1, a, b};
 }
-inline TileSet only(int t) { return TileSet{t, -1, -1}; }
+__host__ __device__ inline TileSet only(int t) { return TileSet{t, -1, -1}; }
 
 // ------------------------------------------------------------ block closure
 // Min-plus closure (the k-sequential Floyd-Warshall sweep) of an NB x NB block

@@ -67,6 +67,8 @@ struct AuxStream {
     cudaEvent_t fork = nullptr;
     cudaEvent_t join = nullptr;
     cudaEvent_t hi_done = nullptr;
+    cudaEvent_t panels[2] = {};   // block t's panels are ready (t & 1)
+    cudaEvent_t bulk[2] = {};     // block t's bulk remainder is done (t & 1)
 };
 int aux_stream_get(cudaStream_t s, AuxStream* out);
 

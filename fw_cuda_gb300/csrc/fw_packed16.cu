@@ -369,16 +369,13 @@ __global__ void __launch_bounds__(kPThreads, 1)
     }
 }
 
-// Remainder tiles (I, J), I from `rows`, J from `cols`, with the 256 pivots of
-// the panels in colD / rowP.
-__global__ void __launch_bounds__(kPThreads, 1)
-    fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, TileSet rows, TileSet cols,
-                            const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP, const P16Status* st,
-                            int one) {
-    if (st->ineligible) return;
+// One tile (r0, w0) of D16 (row r0, word column w0) updated with the 256
+// pivots of the panels in colD / rowP.
+__device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_t ld16, int64_t r0, int64_t w0,
+                                              const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP,
+                                              int one) {
     extern __shared__ __align__(128) uint32_t psm[];
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    const int64_t r0 = (int64_t)tile_of(rows, blockIdx.y) * kPT, w0 = (int64_t)tile_of(cols, blockIdx.x) * kPW;
     const int64_t ldw = ld16 / 2;
     uint32_t c[8][8];
     p_load_tile(c, D16, ldw, r0, w0, tx, ty);
@@ -386,6 +383,36 @@ __global__ void __launch_bounds__(kPThreads, 1)
         c, kPT / kSlab, psm, [&](uint32_t* dst, int s) { p_load_kmajor<kPT>(dst, colD, ld16, s * kSlab, r0, tid); },
         [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, w0, tid); }, tx, ty, one);
     p_store_tile(c, D16, ldw, r0, w0, tx, ty);
+}
+
+// Remainder tiles (I, J), I from `rows`, J from `cols`, with the 256 pivots of
+// the panels in colD / rowP.
+__global__ void __launch_bounds__(kPThreads, 1)
+    fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, TileSet rows, TileSet cols,
+                            const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP, const P16Status* st,
+                            int one) {
+    if (st->ineligible) return;
+    p_update_tile(D16, ld16, (int64_t)tile_of(rows, blockIdx.y) * kPT, (int64_t)tile_of(cols, blockIdx.x) * kPW, colD,
+                  rowP, one);
+}
+
+// Block t's update of block u = t + 1's row and column in one launch: CTAs
+// [0, T - 1) take the row tiles (u, J), J != t; CTAs [T - 1, 2T - 3) the
+// column tiles (I, u), I != t, u.
+__global__ void __launch_bounds__(kPThreads, 1)
+    fw_p16_cross_kernel(uint16_t* __restrict__ D16, int64_t ld16, int t, int T, const uint32_t* __restrict__ colD,
+                        const uint32_t* __restrict__ rowP, const P16Status* st, int one) {
+    if (st->ineligible) return;
+    const int u = t + 1;
+    int I, J;
+    if ((int)blockIdx.x < T - 1) {
+        I = u;
+        J = tile_of(all_but(t), blockIdx.x);
+    } else {
+        I = tile_of(all_but(t, u), blockIdx.x - (T - 1));
+        J = u;
+    }
+    p_update_tile(D16, ld16, (int64_t)I * kPT, (int64_t)J * kPW, colD, rowP, one);
 }
 
 }  // namespace
@@ -402,17 +429,15 @@ size_t p16_workspace_bytes(int64_t n) {
 
 // Enqueues encode, the packed sweep and the guarded decode on `s`; *done_flag
 // receives the device address of the word that tells the int32 kernels to
-// skip. The sweep looks one pivot block ahead: after block t's panels, the
-// tiles of block t+1's row and column get block t's update on `s`, then the
-// other remainder tiles of block t run on a side stream while block t+1 is
-// closed and its panels computed on a high-priority stream (into the other
-// panel buffer); `s` waits for both before block t+1's own remainder.
+// skip. The sweep looks one pivot block ahead (two panel buffers): see the
+// schedule below.
 int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
     static bool attr_done = false;
     if (!attr_done) {
         FW_CUDA_TRY(cudaFuncSetAttribute(fw_p16_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
         FW_CUDA_TRY(
             cudaFuncSetAttribute(fw_p16_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+        FW_CUDA_TRY(cudaFuncSetAttribute(fw_p16_cross_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
         attr_done = true;
     }
     AuxStream aux;
@@ -469,27 +494,45 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
         return FW_OK;
     };
 
-    if (int rc = close(0, s)) return rc;
+    // Block t's row and column update of block t + 1 (one launch).
+    auto cross = [&](int t, cudaStream_t q) -> int {
+        const int b = t & 1, u = t + 1;
+        prof_begin(KC_P16_REMAINDER, q);
+        fw_p16_cross_kernel<<<(unsigned)(2 * T - 3), kPThreads, kPSmemBytes, q>>>(D16, ld, t, T, colD[b], rowP[b], st,
+                                                                                 1);
+        FW_LAUNCH_CHECK("fw_p16_cross_kernel");
+        prof_end(KC_P16_REMAINDER, q, (kv(u) * ((double)n - kv(t)) + ((double)n - kv(t) - kv(u)) * kv(u)) * kv(t));
+        return FW_OK;
+    };
+
+    // Schedule: the high-priority stream carries the chain that every later
+    // block waits for — block t's update of block t+1's row and column, then
+    // block t+1's closure and panels — while the side stream runs block t's
+    // bulk remainder (every tile outside both blocks) concurrently. The chain
+    // for block t+1 starts once the bulk of block t-1 is done (its tiles, and
+    // the panel buffer block t+1 reuses).
+    FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
+    FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
+    FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+    if (int rc = close(0, aux.hi)) return rc;
+    FW_CUDA_TRY(cudaEventRecord(aux.panels[0], aux.hi));
     for (int t = 0; t < T; ++t) {
-        if (t + 1 >= T) {
-            if (int rc = remainder(t, all_but(t), T - 1, all_but(t), T - 1, s)) return rc;
-            break;
+        if (t + 1 < T) {
+            if (t >= 1) FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.bulk[(t - 1) & 1], 0));
+            if (int rc = cross(t, aux.hi)) return rc;
+            if (int rc = close(t + 1, aux.hi)) return rc;
+            FW_CUDA_TRY(cudaEventRecord(aux.panels[(t + 1) & 1], aux.hi));
         }
-        // block t's update of block t+1's row (all columns but t) and column
-        if (int rc = remainder(t, only(t + 1), 1, all_but(t), T - 1, s)) return rc;
-        if (int rc = remainder(t, all_but(t, t + 1), T - 2, only(t + 1), 1, s)) return rc;
-        // the rest of block t's remainder on the side stream ...
-        FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
-        FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
-        FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
-        if (int rc = remainder(t, all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, aux.side)) return rc;
-        FW_CUDA_TRY(cudaEventRecord(aux.join, aux.side));
-        // ... while block t+1 is closed on the high-priority stream
-        if (int rc = close(t + 1, aux.hi)) return rc;
-        FW_CUDA_TRY(cudaEventRecord(aux.hi_done, aux.hi));
-        FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.hi_done, 0));
-        FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.join, 0));
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.panels[t & 1], 0));
+        if (t + 1 < T) {
+            if (int rc = remainder(t, all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, aux.side)) return rc;
+        } else {
+            if (int rc = remainder(t, all_but(t), T - 1, all_but(t), T - 1, aux.side)) return rc;
+        }
+        FW_CUDA_TRY(cudaEventRecord(aux.bulk[t & 1], aux.side));
     }
+    // The side stream's last launch follows every launch of the chain.
+    FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.bulk[(T - 1) & 1], 0));
     fw_p16_rmax_kernel<<<grid, 256, 0, s>>>(D16, n, ld, st);
     FW_LAUNCH_CHECK("fw_p16_rmax_kernel");
     fw_p16_decode_kernel<<<grid, 256, 0, s>>>(D16, D, n, ld, st);
