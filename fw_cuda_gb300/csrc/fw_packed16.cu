@@ -256,6 +256,80 @@ __device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint3
     }
 }
 
+// ------------------------------------------------------------ diagonal closure
+// Thread (tx, ty) holds rows ty*4 + {0..3} and 128 + ty*4 + {0..3}, words
+// tx*4 + {0..3} and 64 + tx*4 + {0..3} of the 256 x 256 block. Pivot k's row
+// is row r = (k >= 128 ? 4 : 0) + k % 4 of ty = (k % 128) / 4; its column is
+// half k % 2 of word w = (k >= 128 ? 4 : 0) + (k / 2) % 4 of tx = (k % 128) / 8.
+// The owners publish pivot k + 1 into the other buffer after relaxing pivot k.
+template <int RS, int WS, int HALF>
+__device__ __forceinline__ void p_publish(const uint32_t (&c)[8][8], uint32_t* prw_next, uint32_t* pcl_next,
+                                          bool row_owner, bool col_owner, int tx, int ty) {
+    if (row_owner) {
+        *reinterpret_cast<uint4*>(prw_next + tx * 4) = make_uint4(c[RS][0], c[RS][1], c[RS][2], c[RS][3]);
+        *reinterpret_cast<uint4*>(prw_next + 64 + tx * 4) = make_uint4(c[RS][4], c[RS][5], c[RS][6], c[RS][7]);
+    }
+    if (col_owner) {
+        uint32_t v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = dup16(HALF ? (c[r][WS] >> 16) : (c[r][WS] & 0xFFFFu));
+        *reinterpret_cast<uint4*>(pcl_next + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<uint4*>(pcl_next + 128 + ty * 4) = make_uint4(v[4], v[5], v[6], v[7]);
+    }
+}
+
+// Pivot UPPER * 128 + kb + U (kb a multiple of 8); U is a template argument so
+// that the owners' register indices are compile-time constants.
+template <int UPPER, int U>
+__device__ __forceinline__ void p_diag_step(uint32_t (&c)[8][8], uint32_t (*prw)[kPW], uint32_t (*pcl)[kPT], int tx,
+                                            int ty, int kb) {
+    constexpr int buf = U & 1;  // k & 1
+    uint32_t a[8], b[8];
+    {
+        const uint4 x0 = *reinterpret_cast<const uint4*>(&pcl[buf][ty * 4]);
+        const uint4 x1 = *reinterpret_cast<const uint4*>(&pcl[buf][128 + ty * 4]);
+        const uint4 y0 = *reinterpret_cast<const uint4*>(&prw[buf][tx * 4]);
+        const uint4 y1 = *reinterpret_cast<const uint4*>(&prw[buf][64 + tx * 4]);
+        a[0] = x0.x; a[1] = x0.y; a[2] = x0.z; a[3] = x0.w; a[4] = x1.x; a[5] = x1.y; a[6] = x1.z; a[7] = x1.w;
+        b[0] = y0.x; b[1] = y0.y; b[2] = y0.z; b[3] = y0.w; b[4] = y1.x; b[5] = y1.y; b[6] = y1.z; b[7] = y1.w;
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int w = 0; w < 8; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
+    uint32_t* prw_next = prw[buf ^ 1];
+    uint32_t* pcl_next = pcl[buf ^ 1];
+    if (U < 7) {
+        // pivot k + 1 = UPPER * 128 + kb + U + 1, same group
+        p_publish<UPPER * 4 + ((U + 1) & 3), UPPER * 4 + ((U + 1) >> 1), (U + 1) & 1>(
+            c, prw_next, pcl_next, ty == ((kb + U + 1) >> 2), tx == (kb >> 3), tx, ty);
+    } else if (!UPPER && kb == 120) {
+        // pivot 128: row 4 of ty 0, low half of word 4 of tx 0
+        p_publish<4, 4, 0>(c, prw_next, pcl_next, ty == 0, tx == 0, tx, ty);
+    } else if (!(UPPER && kb == 120)) {
+        // pivot k + 1 = UPPER * 128 + kb + 8, next group
+        p_publish<UPPER * 4, UPPER * 4, 0>(c, prw_next, pcl_next, ty == ((kb + 8) >> 2), tx == ((kb + 8) >> 3), tx,
+                                           ty);
+    }
+    __syncthreads();
+}
+
+// Pivots UPPER * 128 + [0, 128), eight per group.
+template <int UPPER>
+__device__ __forceinline__ void p_diag_phase(uint32_t (&c)[8][8], uint32_t (*prw)[kPW], uint32_t (*pcl)[kPT], int tx,
+                                             int ty) {
+    for (int kb = 0; kb < 128; kb += 8) {
+        p_diag_step<UPPER, 0>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 1>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 2>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 3>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 4>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 5>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 6>(c, prw, pcl, tx, ty, kb);
+        p_diag_step<UPPER, 7>(c, prw, pcl, tx, ty, kb);
+    }
+}
+
 // ------------------------------------------------------------ kernels
 // Closure of the 256 x 256 pivot block, one CTA; writes D16, colD (transposed,
 // duplicated) and rowP (packed rows) for the block.
@@ -279,45 +353,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
         for (int r = 0; r < 8; ++r) pcl[0][prow_of(ty, r)] = dup16(c[r][0] & 0xFFFFu);
     }
     __syncthreads();
-    for (int kb = 0; kb < kPT; kb += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int k = kb + u, buf = u & 1;
-            uint32_t a[8], b[8];
-#pragma unroll
-            for (int r = 0; r < 8; ++r) a[r] = pcl[buf][prow_of(ty, r)];
-#pragma unroll
-            for (int w = 0; w < 8; ++w) b[w] = prw[buf][pword_of(tx, w)];
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-#pragma unroll
-                for (int w = 0; w < 8; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
-            const int k1 = k + 1;
-            if (k1 < kPT) {
-                // row k1: ty = (k1 % 128) / 4, r = (k1 >= 128 ? 4 : 0) + k1 % 4
-                const int rsel = (u + 1) & 3;
-                const bool upper = k1 >= 128;
-                if (ty == ((k1 & 127) >> 2)) {
-#pragma unroll
-                    for (int w = 0; w < 8; ++w) prw[buf ^ 1][pword_of(tx, w)] = upper ? c[4 + rsel][w] : c[rsel][w];
-                }
-                // column k1: word k1 / 2, half k1 % 2; owner tx = (word % 64) / 4, w = (word >= 64 ? 4 : 0) + word % 4
-                const int word = k1 >> 1, half = k1 & 1;
-                if (tx == ((word & 63) >> 2)) {
-                    const int wsel = (word >= 64 ? 4 : 0) + (word & 3);
-#pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        uint32_t x = 0;
-#pragma unroll
-                        for (int w = 0; w < 8; ++w)
-                            if (w == wsel) x = c[r][w];
-                        pcl[buf ^ 1][prow_of(ty, r)] = dup16(half ? (x >> 16) : (x & 0xFFFFu));
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
+    p_diag_phase<0>(c, prw, pcl, tx, ty);
+    p_diag_phase<1>(c, prw, pcl, tx, ty);
     p_store_tile(c, D16, ldw, p0, p0 / 2, tx, ty);
     p_store_coldup(c, colD, ld16, p0, tx, ty);
     // rowP rows are the pivot rows k = p0.. as packed words, ld = ld16 / 2
