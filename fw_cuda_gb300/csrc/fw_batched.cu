@@ -138,10 +138,12 @@ __device__ __forceinline__ void small_bucket_any(int groups, int* packed, const 
 // ------------------------------------------------------------ one large graph
 // The blocked sweep of one n x n graph by one CTA: per 128-wide pivot block,
 // the diagonal closure, the row and column panels, then the remainder tiles,
-// one tile at a time. colT (128 x ldw ints, this CTA's workspace slice) holds
-// the current column panel transposed.
-__device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int* __restrict__ colT, int64_t ldw,
-                                               int* smem, int one) {
+// one tile at a time. This CTA's workspace slice holds the current panels in
+// the single-graph engine's layout: colT (128 x ldw ints) the column panel
+// transposed, rowP (128 x ldw) the row panel, so the remainder streams both
+// operands with 16-byte cp.async whatever the graph's row alignment.
+__device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int* __restrict__ colT,
+                                               int* __restrict__ rowP, int64_t ldw, int* smem, int one) {
     using Closure = BlockClosure<kTile, 16, 16>;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int T = (n + kTile - 1) / kTile;
@@ -177,6 +179,8 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
                 for (int r = 0; r < 8; ++r) col[r] = c[r][e];
                 st_vec<8>(colT + (int64_t)(tx * 8 + e) * ldw + p0 + ty * 8, col);
             }
+#pragma unroll
+            for (int r = 0; r < 8; ++r) st_vec<8>(rowP + (int64_t)(ty * 8 + r) * ldw + p0 + tx * 8, c[r]);
             __syncthreads();
         }
         int acc[8][8];
@@ -189,6 +193,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
                 acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, p0, tid); },
                 [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
             store_acc<false>(acc, Gm, n, p0, q0, tx, ty);
+            store_acc_ws(acc, rowP, ldw, q0, tx, ty);
             __syncthreads();
         }
         // 3. column panel: D[I][P] = min(D[I][P], D[I][P] (x) Dg*), also into colT
@@ -199,7 +204,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
             mainloop<kMixA>(
                 acc, nslab, smem,
                 [&](int* dst, int s) { load_d_transposed<false>(dst, Gm, n, r0, p0 + s * kSlab, tid); },
-                [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, p0, tid); }, tx, ty, one);
+                [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, p0, tid); }, tx, ty, one);
             store_acc<false>(acc, Gm, n, r0, p0, tx, ty);
             store_acc_ws_transposed(acc, colT, ldw, r0, tx, ty);
             __syncthreads();
@@ -214,7 +219,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
                 load_acc<false>(acc, Gm, n, r0, q0, tx, ty);
                 mainloop<kMixA>(
                     acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, r0, tid); },
-                    [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
+                    [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, q0, tid); }, tx, ty, one);
                 store_acc<false>(acc, Gm, n, r0, q0, tx, ty);
                 __syncthreads();
             }
@@ -228,7 +233,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     extern __shared__ __align__(128) int smem[];
     __shared__ int s_item[8];
     // bucket 0: whole CTA per graph
-    int* colT = ws + (int64_t)blockIdx.x * kTile * ldw;
+    int* colT = ws + (int64_t)blockIdx.x * 2 * kTile * ldw;
+    int* rowP = colT + (int64_t)kTile * ldw;
     for (;;) {
         if (threadIdx.x == 0) s_item[0] = atomicAdd(&counters[0], 1);
         __syncthreads();
@@ -236,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         __syncthreads();
         if (it >= sched.count[0]) break;
         const BatchItem item = items[sched.start[0] + it];
-        blocked_in_cta(packed + item.offset, item.n, colT, ldw, smem, one);
+        blocked_in_cta(packed + item.offset, item.n, colT, rowP, ldw, smem, one);
     }
     small_bucket<128, 1>(packed, items, sched.start[1], sched.count[1], &counters[1], smem, s_item);
     __syncthreads();
@@ -390,7 +396,7 @@ int fw_batch_plan_create(fw_batch_plan** out, const int32_t* h_sizes, const int6
         }
         if (cudaMalloc(&p->d_items, sizeof(BatchItem) * count) != cudaSuccess ||
             cudaMalloc(&p->d_counters, sizeof(int) * kBuckets) != cudaSuccess ||
-            cudaMalloc(&p->d_ws, sizeof(int) * (size_t)kTile * p->ldw * p->ws_ctas) != cudaSuccess) {
+            cudaMalloc(&p->d_ws, sizeof(int) * (size_t)2 * kTile * p->ldw * p->ws_ctas) != cudaSuccess) {
             cudaGetLastError();
             rc = set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_create: device allocation failed");
             break;
