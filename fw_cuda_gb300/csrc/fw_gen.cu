@@ -15,7 +15,7 @@
 //     with r = x^J mod phi (Haramoto et al., 2008, polynomial jump-ahead),
 //     so with r_c = (x^L)^c mod phi every chunk of L = 2^25 outputs gets its
 //     starting state from the seeded first 20560 words, one CTA per chunk
-//     (fw_gen_jump_kernel), and one warp per chunk then runs the recurrence
+//     (fw_gen_jump_kernel), and one CTA per chunk then runs the recurrence
 //     227 words at a time (fw_gen_words_kernel).
 //  2. Parse. A pair takes 2 words (the bernoulli draw: libstdc++'s
 //     generate_canonical<double, 53> reads two 32-bit words) plus, for an
@@ -45,6 +45,7 @@
 #include <mutex>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fw_common.cuh"
@@ -60,7 +61,7 @@ constexpr int kMtDeg = 19937;                      // degree of phi
 constexpr int kPolyWords = (kMtDeg + 63) / 64;     // 312
 constexpr int kBaseWords = kMtDeg + kMtN - 1;      // x[0 .. 19936 + 623]
 constexpr int kChunkLog2 = 25;
-constexpr uint64_t kChunk = uint64_t(1) << kChunkLog2;  // outputs per generating warp
+constexpr uint64_t kChunk = uint64_t(1) << kChunkLog2;  // outputs per generating CTA
 constexpr int kStep = kMtN - kMtM;                 // 227 words per step of the recurrence
 
 __host__ __device__ __forceinline__ uint32_t mt_next(uint32_t xk, uint32_t xk1, uint32_t xm) {
@@ -202,6 +203,18 @@ struct Gf2Mod {
     }
 };
 
+// g^e mod phi by square-and-multiply.
+Poly g_power(const Gf2Mod& f, const Poly& g, uint64_t e) {
+    Poly acc(kPolyWords, 0), base = g;
+    acc[0] = 1;
+    while (e) {
+        if (e & 1) acc = f.mul(acc, base);
+        e >>= 1;
+        if (e) base = f.sqr(base);
+    }
+    return acc;
+}
+
 // Process-wide jump tables: phi, g = x^kChunk mod phi and r_c = g^c.
 struct JumpTables {
     std::mutex mu;
@@ -262,7 +275,32 @@ int ensure_jump_tables(size_t chunks) {
         t.r.push_back(one);
         t.ready = true;
     }
-    while (t.r.size() < chunks) t.r.push_back(t.field.mul(t.r.back(), t.g));
+    // r[c] = g^c for the missing c, split over host threads: each thread
+    // starts its contiguous range with one exponentiation and walks it with
+    // one multiplication per entry.
+    const size_t have = t.r.size();
+    if (have < chunks) {
+        t.r.resize(chunks);
+        const size_t todo = chunks - have;
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t workers = std::min<size_t>({(size_t)hw, (size_t)16, (todo + 3) / 4});
+        const size_t per = (todo + workers - 1) / workers;
+        auto fill = [&](size_t lo, size_t hi) {
+            Poly acc = t.r[lo - 1];
+            if (lo - 1 >= have) acc = g_power(t.field, t.g, lo - 1);
+            for (size_t c = lo; c < hi; ++c) {
+                acc = t.field.mul(acc, t.g);
+                t.r[c] = acc;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t w = 1; w < workers; ++w) {
+            const size_t lo = have + w * per, hi = std::min(chunks, have + (w + 1) * per);
+            if (lo < hi) pool.emplace_back(fill, lo, hi);
+        }
+        fill(have, std::min(chunks, have + per));
+        for (auto& th : pool) th.join();
+    }
     return FW_OK;
 }
 
@@ -434,29 +472,25 @@ __global__ void __launch_bounds__(640) fw_gen_jump_kernel(const uint32_t* __rest
     states[(size_t)blockIdx.x * kMtN + t] = acc;
 }
 
-// One warp per chunk of kChunk outputs: the recurrence on a 1024-word ring in
-// shared memory, 227 new words per step (they read only words of the
-// previous 624, which the step does not overwrite).
-constexpr int kGenWarps = 4;
-__global__ void __launch_bounds__(32 * kGenWarps) fw_gen_words_kernel(const uint32_t* __restrict__ states, int chunks,
-                                                                      uint32_t* __restrict__ out) {
-    __shared__ uint32_t ring[kGenWarps][1024];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * kGenWarps + warp;
-    if (c >= chunks) return;
-    uint32_t* rg = ring[warp];
-    for (int t = lane; t < kMtN; t += 32) rg[t] = states[(size_t)c * kMtN + t];
-    __syncwarp();
+// One CTA per chunk of kChunk outputs: the recurrence on a 1024-word ring in
+// shared memory, 227 new words per step, one per thread (they read only words
+// of the previous 624, which the step does not overwrite).
+constexpr int kGenThreads = 256;
+__global__ void __launch_bounds__(kGenThreads) fw_gen_words_kernel(const uint32_t* __restrict__ states,
+                                                                   uint32_t* __restrict__ out) {
+    __shared__ uint32_t rg[1024];
+    const int c = blockIdx.x, t = threadIdx.x;
+    for (int i = t; i < kMtN; i += kGenThreads) rg[i] = states[(size_t)c * kMtN + i];
+    __syncthreads();
     uint32_t* o = out + (uint64_t)c * kChunk;
     for (uint32_t k0 = 0; k0 < (uint32_t)kChunk; k0 += kStep) {
-        const uint32_t cnt = min((uint32_t)kStep, (uint32_t)kChunk - k0);
-        for (uint32_t t = lane; t < cnt; t += 32) {
-            const uint32_t k = k0 + t;
+        const uint32_t k = k0 + (uint32_t)t;
+        if (t < kStep && k < (uint32_t)kChunk) {
             const uint32_t xn = mt_next(rg[k & 1023], rg[(k + 1) & 1023], rg[(k + kMtM) & 1023]);
             rg[(k + kMtN) & 1023] = xn;
             o[k] = mt_temper(xn);
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -646,7 +680,7 @@ int generate_attempt(int32_t* d_D, int64_t n, const GenParams& gp, const std::ve
     FW_CUDA_TRY(cudaFuncSetAttribute(fw_gen_jump_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jump_smem));
     fw_gen_jump_kernel<<<(unsigned)chunks, 640, jump_smem, s>>>(d_base, d_polys, d_states);
     FW_LAUNCH_CHECK("fw_gen_jump_kernel");
-    fw_gen_words_kernel<<<grid_for(chunks, kGenWarps), 32 * kGenWarps, 0, s>>>(d_states, (int)chunks, d_words);
+    fw_gen_words_kernel<<<(unsigned)chunks, kGenThreads, 0, s>>>(d_states, d_words);
     FW_LAUNCH_CHECK("fw_gen_words_kernel");
 
     unsigned* d_err = reinterpret_cast<unsigned*>(d_status + 1);
@@ -718,14 +752,18 @@ int fw_generate_graph_device_i32(int32_t* d_D, int64_t n, double density, uint32
 
 int fw_mt19937_outputs(uint32_t seed, uint64_t skip, int64_t count, uint32_t* h_out) {
     if (h_out == nullptr || count < 0) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_mt19937_outputs: bad arguments");
-    if (int rc = ensure_jump_tables(1)) return rc;
+    // skip = c * kChunk + rem: the chunk table entry r_c (the one the device
+    // generator uses for chunk c) times x^rem.
+    const uint64_t c = skip / kChunk, rem = skip % kChunk;
+    if (c > (1u << 20)) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_mt19937_outputs: skip too large");
+    if (int rc = ensure_jump_tables((size_t)c + 1)) return rc;
     std::vector<uint32_t> base;
     mt_sequence(seed, base, kBaseWords);
     Poly r;
     {
         JumpTables& t = jump_tables();
         std::lock_guard<std::mutex> lk(t.mu);
-        r = x_pow(skip);
+        r = t.field.mul(t.r[(size_t)c], x_pow(rem));
     }
     std::vector<uint32_t> x(kMtN);
     jumped_state(base, r, x.data());

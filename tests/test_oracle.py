@@ -143,7 +143,7 @@ def test_mt19937_jump_ahead_matches_std(fw, oracle):
     (host side of fw_generate_graph_device_i32); its outputs after a skip
     equal std::mt19937 after discard(skip)."""
     for seed, skip in [(5489, 0), (42, 1), (42, 623), (42, 624), (7, 625), (123, 2**25),
-                       (99, 3 * 2**25 + 17), (7, 2**28 + 12345)]:
+                       (99, 3 * 2**25 + 17), (7, 2**28 + 12345), (11, 40 * 2**25 + 5)]:
         count = 1500
         assert np.array_equal(fw.mt19937_outputs(seed, skip, count),
                               oracle.mt19937_outputs(seed, skip, count)), (seed, skip)
