@@ -197,7 +197,7 @@ namespace fw {
 size_t min_workspace_bytes(int64_t n, int kappa, int variant) {
     if (n < 1) return 0;
     if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
-    const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa));
+    const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa, n));
     if (variant == FW_VARIANT_AUTO) return ((blocked_workspace_bytes(n, 2) + 255) & ~size_t(255)) + p16_workspace_bytes(n);
     return blocked;
 }
@@ -218,7 +218,7 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
         return set_error(FW_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
-    const int blocks = blocks_per_pass(variant, kappa);
+    const int blocks = blocks_per_pass(variant, kappa, n);
     if (variant == FW_VARIANT_AUTO) {
         const size_t blocked = (blocked_workspace_bytes(n, 2) + 255) & ~size_t(255);
         const unsigned int* done = nullptr;

@@ -76,7 +76,7 @@ int aux_stream_get(cudaStream_t s, AuxStream* out);
 int normalise_kappa(int kappa);
 
 // Blocked-sweep launchers (fw_apsp_i32.cu).
-int blocks_per_pass(int variant, int kappa);
+int blocks_per_pass(int variant, int kappa, int64_t n);
 size_t blocked_workspace_bytes(int64_t n, int blocks);
 // `skip`, when not null, is a device flag: nonzero makes every kernel of the
 // sweep return at once (the packed fast path already produced the result).
