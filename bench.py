@@ -326,7 +326,22 @@ def run_ours(args) -> None:
     except OSError:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    if used_packed:
+    if variant == VARIANTS["baseline_gpu"]:
+        st = prof.get("fw_pivot_step")
+        roofline = None
+        if st and st["launches"]:
+            secs = st["total_ms"] / 1e3
+            # algorithmic bytes of a pivot launch: the matrix read once (4 n^2);
+            # writes are the entries that change, which the kernel alone stores
+            gbs = 4.0 * n * n * st["launches"] / secs / 1e9
+            roofline = {"kernel": "fw_pivot_step_vec_kernel" if n % 4 == 0 else "fw_pivot_step_kernel",
+                        "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                        else "fallback", "avg_launch_ms": st["total_ms"] / st["launches"],
+                        "traffic": (268.54e6 + 3.45e6) * (n / 8192.0) ** 2, "traffic_unit": "bytes per launch",
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of pivot 4000 at "
+                                          "n = 8192, scaled by n^2"}
+    elif used_packed:
         roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, 512, peak_packed,
                                "measured live: register-only packed 16-bit DPX add-min kernel "
                                "(fw_measure_relax_peak_packed)", hbm_peak, "hbm_gbs" in peaks,
@@ -334,7 +349,7 @@ def run_ours(args) -> None:
         if roofline:
             roofline["int32_dpx_only_peak"] = peak_dpx
     else:
-        pair = variant == VARIANTS["multi_layer_tiling_gpu"] and args.kappa > 4
+        pair = variant == VARIANTS["multi_layer_tiling_gpu"] and args.kappa > 4 and n >= 24576
         # bulk launch: all tiles outside two pivot blocks (the two-block pass,
         # or the look-ahead of the one-block pass)
         roofline = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 256 if pair else 128, 4,

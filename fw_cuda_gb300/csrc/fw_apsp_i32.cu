@@ -191,8 +191,7 @@ __global__ void fw_pivot_prime_kernel(const int* __restrict__ D, int64_t n, int*
 
 // Pivot k over row blockIdx.y: D[i][j] = min(D[i][j], colk[i] + rowk[j]);
 // row k + 1 and column k + 1 of the result go to the next snapshot. Stores
-// only vectors that changed.
-template <bool VEC>
+// only values that changed. Scalar form, for n % 4 != 0.
 __global__ void __launch_bounds__(256)
     fw_pivot_step_kernel(int* __restrict__ D, int64_t n, int64_t k, const int* __restrict__ rowk,
                          const int* __restrict__ colk, int* __restrict__ rown, int* __restrict__ coln) {
@@ -200,31 +199,63 @@ __global__ void __launch_bounds__(256)
     const int dik = colk[i];
     int* row = D + i * n;
     const bool next_row = (i == k + 1);
-    if (VEC) {
-        const int64_t n4 = n >> 2;
-        for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (int64_t)gridDim.x * blockDim.x) {
-            const int4 b = *reinterpret_cast<const int4*>(rowk + q * 4);
-            const int4 d = *reinterpret_cast<const int4*>(row + q * 4);
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int d = row[j];
+        const int o = __viaddmin_s32(dik, rowk[j], d);
+        if (o != d) row[j] = o;
+        if (next_row) rown[j] = o;
+        if (j == k + 1) coln[i] = o;
+    }
+}
+
+// Vector form for n % 4 == 0: a CTA takes kPivRows rows and a chunk of
+// 256 * kPivVecs 16-byte vectors of them, so every thread loads its pivot-row
+// vectors once for kPivRows rows; 32-bit vector indices, and only the thread
+// whose vector holds column k + 1 writes the column snapshot.
+constexpr int kPivRows = 4, kPivVecs = 4;
+__global__ void __launch_bounds__(256)
+    fw_pivot_step_vec_kernel(int* __restrict__ D, int64_t n, int k, const int* __restrict__ rowk,
+                             const int* __restrict__ colk, int* __restrict__ rown, int* __restrict__ coln) {
+    const int n4 = (int)(n >> 2);
+    const int qk1 = (k + 1) >> 2, ek1 = (k + 1) & 3;
+    int4 b[kPivVecs];
+    int qs[kPivVecs];
+#pragma unroll
+    for (int v = 0; v < kPivVecs; ++v) {
+        qs[v] = (blockIdx.x * kPivVecs + v) * 256 + threadIdx.x;
+        if (qs[v] < n4) b[v] = *reinterpret_cast<const int4*>(rowk + 4 * (int64_t)qs[v]);
+    }
+    // all loads first, so that each thread has kPivRows * kPivVecs 16-byte
+    // loads in flight
+    int dik[kPivRows];
+    int4 d[kPivRows][kPivVecs];
+    const int64_t i0 = (int64_t)blockIdx.y * kPivRows;
+#pragma unroll
+    for (int r = 0; r < kPivRows; ++r) {
+        dik[r] = (i0 + r < n) ? colk[i0 + r] : 0;
+#pragma unroll
+        for (int v = 0; v < kPivVecs; ++v)
+            if (i0 + r < n && qs[v] < n4) d[r][v] = *reinterpret_cast<const int4*>(D + (i0 + r) * n + 4 * (int64_t)qs[v]);
+    }
+#pragma unroll
+    for (int r = 0; r < kPivRows; ++r) {
+        const int64_t i = i0 + r;
+        if (i >= n) break;
+        int* row = D + i * n;
+        const bool next_row = (i == (int64_t)k + 1);
+#pragma unroll
+        for (int v = 0; v < kPivVecs; ++v) {
+            const int q = qs[v];
+            if (q >= n4) continue;
             int4 o;
-            o.x = __viaddmin_s32(dik, b.x, d.x);
-            o.y = __viaddmin_s32(dik, b.y, d.y);
-            o.z = __viaddmin_s32(dik, b.z, d.z);
-            o.w = __viaddmin_s32(dik, b.w, d.w);
-            if (o.x != d.x || o.y != d.y || o.z != d.z || o.w != d.w) *reinterpret_cast<int4*>(row + q * 4) = o;
-            if (next_row) *reinterpret_cast<int4*>(rown + q * 4) = o;
-            const int64_t j0 = q * 4;
-            if (k + 1 >= j0 && k + 1 < j0 + 4) {
-                const int e = (int)(k + 1 - j0);
-                coln[i] = e == 0 ? o.x : e == 1 ? o.y : e == 2 ? o.z : o.w;
-            }
-        }
-    } else {
-        for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-            const int d = row[j];
-            const int o = __viaddmin_s32(dik, rowk[j], d);
-            if (o != d) row[j] = o;
-            if (next_row) rown[j] = o;
-            if (j == k + 1) coln[i] = o;
+            o.x = __viaddmin_s32(dik[r], b[v].x, d[r][v].x);
+            o.y = __viaddmin_s32(dik[r], b[v].y, d[r][v].y);
+            o.z = __viaddmin_s32(dik[r], b[v].z, d[r][v].z);
+            o.w = __viaddmin_s32(dik[r], b[v].w, d[r][v].w);
+            if (o.x != d[r][v].x || o.y != d[r][v].y || o.z != d[r][v].z || o.w != d[r][v].w)
+                *reinterpret_cast<int4*>(row + 4 * (int64_t)q) = o;
+            if (next_row) *reinterpret_cast<int4*>(rown + 4 * (int64_t)q) = o;
+            if (q == qk1) coln[i] = ek1 == 0 ? o.x : ek1 == 1 ? o.y : ek1 == 2 ? o.z : o.w;
         }
     }
 }
@@ -444,17 +475,18 @@ int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
     fw_pivot_prime_kernel<<<(unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), 256, 0, s>>>(D, n, rowb[0],
                                                                                                     colb[0]);
     FW_LAUNCH_CHECK("fw_pivot_prime_kernel");
-    const int64_t work = vec ? n / 4 : n;
-    const unsigned gx = (unsigned)((work + 255) / 256 < 64 ? (work + 255) / 256 : 64);
+    const unsigned gx = (unsigned)((n + 255) / 256 < 64 ? (n + 255) / 256 : 64);
+    const dim3 vgrid((unsigned)((n / 4 + 256 * kPivVecs - 1) / (256 * kPivVecs)),
+                     (unsigned)((n + kPivRows - 1) / kPivRows));
     for (int64_t k = 0; k < n; ++k) {
         const int cur = (int)(k & 1);
         prof_begin(KC_PIVOT_STEP, s);
         if (vec)
-            fw_pivot_step_kernel<true><<<dim3(gx, (unsigned)n), 256, 0, s>>>(D, n, k, rowb[cur], colb[cur],
-                                                                             rowb[cur ^ 1], colb[cur ^ 1]);
+            fw_pivot_step_vec_kernel<<<vgrid, 256, 0, s>>>(D, n, (int)k, rowb[cur], colb[cur], rowb[cur ^ 1],
+                                                           colb[cur ^ 1]);
         else
-            fw_pivot_step_kernel<false><<<dim3(gx, (unsigned)n), 256, 0, s>>>(D, n, k, rowb[cur], colb[cur],
-                                                                              rowb[cur ^ 1], colb[cur ^ 1]);
+            fw_pivot_step_kernel<<<dim3(gx, (unsigned)n), 256, 0, s>>>(D, n, k, rowb[cur], colb[cur], rowb[cur ^ 1],
+                                                                       colb[cur ^ 1]);
         FW_LAUNCH_CHECK("fw_pivot_step_kernel");
         prof_end(KC_PIVOT_STEP, s, (double)n * n);
     }
