@@ -334,12 +334,16 @@ __global__ void __launch_bounds__(kFThreads, 1)
     }
 }
 
-// Phase 3: remainder tile (I, J) of graph blockIdx.z.
+// Phase 3: remainder tiles of graph blockIdx.z with the panels of pivot block
+// pt: tiles (I, J), I from `rows` (nrows), J from `cols` (ncols), one per
+// blockIdx.x; or, with cross >= 0, block pt's update of block u = pt + 1's
+// row and column: tiles [0, T - 1) are (u, J), J != pt, the next T - 2 are
+// (I, u), I != pt, u.
 template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
-    fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt,
-                           const V* __restrict__ colTall, const int* __restrict__ colHall,
-                           const V* __restrict__ rowPall) {
+    fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt, int T,
+                           TileSet rows, TileSet cols, int ncols, int cross, const V* __restrict__ colTall,
+                           const int* __restrict__ colHall, const V* __restrict__ rowPall) {
     extern __shared__ __align__(128) int smem[];
     const int64_t gph = blockIdx.z;
     V* D = Dall + gph * n * n;
@@ -348,8 +352,18 @@ __global__ void __launch_bounds__(kFThreads, 1)
     const int* colH = colHall + gph * kTile * ldp;
     const V* rowP = rowPall + gph * kTile * ldp;
     const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
-    const int ti = (int)blockIdx.y < pt ? (int)blockIdx.y : (int)blockIdx.y + 1;
-    const int tj = (int)blockIdx.x < pt ? (int)blockIdx.x : (int)blockIdx.x + 1;
+    const int x = (int)blockIdx.x;
+    int ti, tj;
+    if (cross < 0) {
+        ti = tile_of(rows, x / ncols);
+        tj = tile_of(cols, x % ncols);
+    } else if (x < T - 1) {
+        ti = pt + 1;
+        tj = tile_of(all_but(pt), x);
+    } else {
+        ti = tile_of(all_but(pt, pt + 1), x - (T - 1));
+        tj = pt + 1;
+    }
     const int64_t p0 = (int64_t)pt * kTile, r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
     const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
     V c[8][4];
@@ -410,11 +424,18 @@ __global__ void __launch_bounds__(256)
 
 }  // namespace
 
+// Two panel buffers (colT, colH, rowP each) per graph: the look-ahead closes
+// block t + 1 into one while block t's remainder reads the other.
 size_t f32_workspace_bytes(int64_t n, int64_t batch) {
     const int64_t ldp = (n + kTile - 1) / kTile * kTile;
-    return (size_t)3 * kTile * ldp * 4 * (size_t)batch;
+    return (size_t)2 * 3 * kTile * ldp * 4 * (size_t)batch;
 }
 
+// The blocked sweep with next hops over a batch of graphs, with a one-block
+// look-ahead: the high-priority stream carries block t's update of block
+// t+1's row and column, block t+1's closure and panels (into the other panel
+// buffer), while the side stream runs block t's bulk remainder (tiles outside
+// both blocks). The chain for block t+1 starts once block t-1's bulk is done.
 template <typename V>
 int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, KernelClass kc) {
     static bool attr_done = false;
@@ -425,28 +446,69 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
             cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
         attr_done = true;
     }
+    AuxStream aux;
+    if (int rc = aux_stream_get(s, &aux)) return rc;
     const int T = (int)((n + kTile - 1) / kTile);
     const int64_t ldp = (int64_t)T * kTile;
-    V* colT = static_cast<V*>(ws);
-    int* colH = reinterpret_cast<int*>(colT + (size_t)kTile * ldp * batch);
-    V* rowP = reinterpret_cast<V*>(colH + (size_t)kTile * ldp * batch);
+    const size_t panel = (size_t)kTile * ldp * batch;
+    V* colT[2];
+    int* colH[2];
+    V* rowP[2];
+    for (int b = 0; b < 2; ++b) {
+        colT[b] = reinterpret_cast<V*>(static_cast<char*>(ws) + (size_t)b * 3 * panel * 4);
+        colH[b] = reinterpret_cast<int*>(colT[b] + panel);
+        rowP[b] = reinterpret_cast<V*>(colH[b] + panel);
+    }
+    const unsigned nb = (unsigned)batch;
+    auto close = [&](int t, cudaStream_t q) -> int {
+        const int b = t & 1;
+        fw_nh_diag_kernel<V><<<dim3(1, 1, nb), kFThreads, 0, q>>>(D, nh, n, ldp, (int64_t)t * kTile, colT[b], colH[b],
+                                                                  rowP[b]);
+        FW_LAUNCH_CHECK("fw_nh_diag_kernel");
+        if (T > 1) {
+            fw_nh_panel_kernel<V><<<dim3(T - 1, 2, nb), kFThreads, kFSmemBytes, q>>>(D, nh, n, ldp, t, colT[b],
+                                                                                     colH[b], rowP[b]);
+            FW_LAUNCH_CHECK("fw_nh_panel_kernel");
+        }
+        return FW_OK;
+    };
+    auto remainder = [&](int t, TileSet rows, int nrows, TileSet cols, int ncols, int cross, cudaStream_t q) -> int {
+        const int tiles = cross >= 0 ? 2 * T - 3 : nrows * ncols;
+        if (tiles <= 0) return FW_OK;
+        const int b = t & 1;
+        fw_nh_remainder_kernel<V><<<dim3((unsigned)tiles, 1, nb), kFThreads, kFSmemBytes, q>>>(
+            D, nh, n, ldp, t, T, rows, cols, ncols, cross, colT[b], colH[b], rowP[b]);
+        FW_LAUNCH_CHECK("fw_nh_remainder_kernel");
+        return FW_OK;
+    };
+
     const int64_t total = n * n * batch;
     prof_begin(kc, s);
     fw_nh_init_kernel<V><<<(unsigned)std::min<int64_t>((total + 255) / 256, 4096), 256, 0, s>>>(D, nh, n, total);
     FW_LAUNCH_CHECK("fw_nh_init_kernel");
-    for (int pt = 0; pt < T; ++pt) {
-        const int64_t p0 = (int64_t)pt * kTile;
-        fw_nh_diag_kernel<V><<<dim3(1, 1, (unsigned)batch), kFThreads, 0, s>>>(D, nh, n, ldp, p0, colT, colH, rowP);
-        FW_LAUNCH_CHECK("fw_nh_diag_kernel");
-        if (T > 1) {
-            fw_nh_panel_kernel<V><<<dim3(T - 1, 2, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(D, nh, n, ldp, pt,
-                                                                                               colT, colH, rowP);
-            FW_LAUNCH_CHECK("fw_nh_panel_kernel");
-            fw_nh_remainder_kernel<V><<<dim3(T - 1, T - 1, (unsigned)batch), kFThreads, kFSmemBytes, s>>>(
-                D, nh, n, ldp, pt, colT, colH, rowP);
-            FW_LAUNCH_CHECK("fw_nh_remainder_kernel");
+    FW_CUDA_TRY(cudaEventRecord(aux.fork, s));
+    FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.fork, 0));
+    FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.fork, 0));
+    if (int rc = close(0, aux.hi)) return rc;
+    FW_CUDA_TRY(cudaEventRecord(aux.panels[0], aux.hi));
+    const TileSet none{-1, -1, -1};
+    for (int t = 0; t < T; ++t) {
+        if (t + 1 < T) {
+            if (t >= 1) FW_CUDA_TRY(cudaStreamWaitEvent(aux.hi, aux.bulk[(t - 1) & 1], 0));
+            if (int rc = remainder(t, none, 0, none, 0, t, aux.hi)) return rc;
+            if (int rc = close(t + 1, aux.hi)) return rc;
+            FW_CUDA_TRY(cudaEventRecord(aux.panels[(t + 1) & 1], aux.hi));
         }
+        FW_CUDA_TRY(cudaStreamWaitEvent(aux.side, aux.panels[t & 1], 0));
+        if (t + 1 < T) {
+            if (int rc = remainder(t, all_but(t, t + 1), T - 2, all_but(t, t + 1), T - 2, -1, aux.side)) return rc;
+        } else {
+            if (int rc = remainder(t, all_but(t), T - 1, all_but(t), T - 1, -1, aux.side)) return rc;
+        }
+        FW_CUDA_TRY(cudaEventRecord(aux.bulk[t & 1], aux.side));
     }
+    // the side stream's last launch follows every launch of the chain
+    FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.bulk[(T - 1) & 1], 0));
     prof_end(kc, s, (double)n * n * n * batch);
     return FW_OK;
 }
