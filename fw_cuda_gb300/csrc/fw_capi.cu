@@ -136,8 +136,6 @@ int aux_stream_get(cudaStream_t s, AuxStream* out) {
         FW_CUDA_TRY(cudaStreamCreateWithFlags(&a.side, cudaStreamNonBlocking));
         FW_CUDA_TRY(cudaStreamCreateWithPriority(&a.hi, cudaStreamNonBlocking, greatest));
         FW_CUDA_TRY(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
-        FW_CUDA_TRY(cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming));
-        FW_CUDA_TRY(cudaEventCreateWithFlags(&a.hi_done, cudaEventDisableTiming));
         for (int i = 0; i < 2; ++i) {
             FW_CUDA_TRY(cudaEventCreateWithFlags(&a.panels[i], cudaEventDisableTiming));
             FW_CUDA_TRY(cudaEventCreateWithFlags(&a.bulk[i], cudaEventDisableTiming));

@@ -58,15 +58,14 @@ void* workspace_get(cudaStream_t s, size_t bytes);
 
 // Two non-blocking streams and their events tied to the caller's (device,
 // stream), created on first use and kept: the look-ahead schedules run the
-// bulk remainder of one pivot block on `side` while the next block is closed
-// and its panels computed on `hi`, whose highest priority lets its few CTAs
+// bulk remainder of pivot block t on `side` while `hi` carries the chain the
+// next block waits for (block t's update of block t+1's row and column, then
+// block t+1's closure and panels); its highest priority lets its few CTAs
 // take SMs as soon as remainder CTAs retire.
 struct AuxStream {
     cudaStream_t side = nullptr;  // bulk remainder (default priority)
-    cudaStream_t hi = nullptr;    // next block's closure and panels (highest priority)
-    cudaEvent_t fork = nullptr;
-    cudaEvent_t join = nullptr;
-    cudaEvent_t hi_done = nullptr;
+    cudaStream_t hi = nullptr;    // the chain (highest priority)
+    cudaEvent_t fork = nullptr;   // the caller's stream up to the solve
     cudaEvent_t panels[2] = {};   // block t's panels are ready (t & 1)
     cudaEvent_t bulk[2] = {};     // block t's bulk remainder is done (t & 1)
 };
