@@ -142,7 +142,11 @@ __device__ __forceinline__ void small_bucket_any(int groups, int* packed, const 
 // the single-graph engine's layout: colT (128 x ldw ints) the column panel
 // transposed, rowP (128 x ldw) the row panel, so the remainder streams both
 // operands with 16-byte cp.async whatever the graph's row alignment.
-__device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int* __restrict__ colT,
+// The graph's n x n values sit in G with leading dimension ldg (ldg = n in
+// place; ldg = the padded staging width, a multiple of 128 with INF padding,
+// when VEC), so the tile helpers take ldg as the matrix extent.
+template <bool VEC>
+__device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int64_t ldg, int* __restrict__ colT,
                                                int* __restrict__ rowP, int64_t ldw, int* smem, int one) {
     using Closure = BlockClosure<kTile, 16, 16>;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -159,7 +163,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int j = tx * 8 + e;
-                    c[r][e] = (i < kv && j < kv) ? Gm[(int64_t)(p0 + i) * n + p0 + j] : kInf;
+                    c[r][e] = (i < kv && j < kv) ? Gm[(int64_t)(p0 + i) * ldg + p0 + j] : kInf;
                 }
             }
             Closure::run(c, smem, smem + 2 * kTile, kv, tx, ty, [] { __syncthreads(); });
@@ -169,7 +173,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int j = tx * 8 + e;
-                    if (i < kv && j < kv) Gm[(int64_t)(p0 + i) * n + p0 + j] = c[r][e];
+                    if (i < kv && j < kv) Gm[(int64_t)(p0 + i) * ldg + p0 + j] = c[r][e];
                 }
             }
 #pragma unroll
@@ -188,11 +192,11 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
         for (int tj = 0; tj < T; ++tj) {
             if (tj == pt) continue;
             const int64_t q0 = (int64_t)tj * kTile;
-            load_acc<false>(acc, Gm, n, p0, q0, tx, ty);
+            load_acc<VEC>(acc, Gm, ldg, p0, q0, tx, ty);
             mainloop<kMixA>(
                 acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, p0, tid); },
-                [&](int* dst, int s) { load_d_rows<false>(dst, Gm, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
-            store_acc<false>(acc, Gm, n, p0, q0, tx, ty);
+                [&](int* dst, int s) { load_d_rows<VEC>(dst, Gm, ldg, p0 + s * kSlab, q0, tid); }, tx, ty, one);
+            store_acc<VEC>(acc, Gm, ldg, p0, q0, tx, ty);
             store_acc_ws(acc, rowP, ldw, q0, tx, ty);
             __syncthreads();
         }
@@ -200,12 +204,12 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
         for (int ti = 0; ti < T; ++ti) {
             if (ti == pt) continue;
             const int64_t r0 = (int64_t)ti * kTile;
-            load_acc<false>(acc, Gm, n, r0, p0, tx, ty);
+            load_acc<VEC>(acc, Gm, ldg, r0, p0, tx, ty);
             mainloop<kMixA>(
                 acc, nslab, smem,
-                [&](int* dst, int s) { load_d_transposed<false>(dst, Gm, n, r0, p0 + s * kSlab, tid); },
+                [&](int* dst, int s) { load_d_transposed<VEC>(dst, Gm, ldg, r0, p0 + s * kSlab, tid); },
                 [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, p0, tid); }, tx, ty, one);
-            store_acc<false>(acc, Gm, n, r0, p0, tx, ty);
+            store_acc<VEC>(acc, Gm, ldg, r0, p0, tx, ty);
             store_acc_ws_transposed(acc, colT, ldw, r0, tx, ty);
             __syncthreads();
         }
@@ -216,11 +220,11 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int*
             for (int tj = 0; tj < T; ++tj) {
                 if (tj == pt) continue;
                 const int64_t q0 = (int64_t)tj * kTile;
-                load_acc<false>(acc, Gm, n, r0, q0, tx, ty);
+                load_acc<VEC>(acc, Gm, ldg, r0, q0, tx, ty);
                 mainloop<kMixA>(
                     acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, r0, tid); },
                     [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, q0, tid); }, tx, ty, one);
-                store_acc<false>(acc, Gm, n, r0, q0, tx, ty);
+                store_acc<VEC>(acc, Gm, ldg, r0, q0, tx, ty);
                 __syncthreads();
             }
         }
@@ -232,7 +236,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                       int* __restrict__ counters, int* __restrict__ ws, int64_t ldw, int one) {
     extern __shared__ __align__(128) int smem[];
     __shared__ int s_item[8];
-    // bucket 0: whole CTA per graph
+    // bucket 0: whole CTA per graph, solved in place
     int* colT = ws + (int64_t)blockIdx.x * 2 * kTile * ldw;
     int* rowP = colT + (int64_t)kTile * ldw;
     for (;;) {
@@ -242,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         __syncthreads();
         if (it >= sched.count[0]) break;
         const BatchItem item = items[sched.start[0] + it];
-        blocked_in_cta(packed + item.offset, item.n, colT, rowP, ldw, smem, one);
+        blocked_in_cta<false>(packed + item.offset, item.n, item.n, colT, rowP, ldw, smem, one);
     }
     small_bucket<128, 1>(packed, items, sched.start[1], sched.count[1], &counters[1], smem, s_item);
     __syncthreads();
@@ -401,6 +405,7 @@ int fw_batch_plan_create(fw_batch_plan** out, const int32_t* h_sizes, const int6
             rc = set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_create: device allocation failed");
             break;
         }
+
         if (cudaMemcpy(p->d_items, items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
             rc = cuda_error(cudaGetLastError(), "cudaMemcpy(items)");
             break;
