@@ -30,9 +30,13 @@
 // kept transposed in a workspace as 32-bit words with the 16-bit value in both
 // halves (colD[k][i] = v | v << 16, the A operand of the packed add), the row
 // panel as plain packed rows (rowP[k][*], the B operand).
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdint>
+#include <mutex>
+#include <string>
 
 #include "fw_common.cuh"
 #include "fw_internal.h"
@@ -55,6 +59,7 @@ struct P16Status {
     unsigned int wmax;        // largest finite input entry
     unsigned int rmax;        // largest result entry below CAP
     unsigned int done;        // 1: D holds the decoded packed result
+    unsigned int copy_fault;  // nonzero: a tile copy did not arrive in time (the int32 sweep runs)
 };
 
 __device__ __forceinline__ uint32_t dup16(uint32_t v) { return v | (v << 16); }
@@ -95,7 +100,7 @@ __global__ void fw_p16_encode_kernel(const int* __restrict__ D, int64_t n, uint1
 }
 
 __global__ void fw_p16_rmax_kernel(const uint16_t* __restrict__ D16, int64_t n, int64_t ld16, P16Status* st) {
-    if (st->ineligible) return;
+    if (st->ineligible || st->copy_fault) return;
     unsigned m = 0;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t v = D16[(q / n) * ld16 + q % n];
@@ -107,7 +112,7 @@ __global__ void fw_p16_rmax_kernel(const uint16_t* __restrict__ D16, int64_t n, 
 
 __global__ void fw_p16_decode_kernel(const uint16_t* __restrict__ D16, int* __restrict__ D, int64_t n, int64_t ld16,
                                      P16Status* st) {
-    if (st->ineligible || st->rmax + st->wmax >= kCap) return;  // the int32 sweep runs instead
+    if (st->ineligible || st->copy_fault || st->rmax + st->wmax >= kCap) return;  // the int32 sweep runs instead
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t v = D16[(q / n) * ld16 + q % n];
         D[q] = (v == kCap) ? kInf : (int)v;
@@ -406,19 +411,96 @@ __global__ void __launch_bounds__(kPThreads, 1)
     }
 }
 
+// ------------------------------------------------------------ TMA tile pipeline
+// The remainder and cross tiles stream their operand slabs with the tensor
+// memory accelerator: per 32-pivot slab one 2-D box of the column panel
+// (32 x 256 words) and one of the row panel (32 x 128 words) land in a
+// shared-memory stage and complete a per-stage mbarrier. Every wait is
+// bounded; a copy that does not arrive sets copy_fault, the packed result is
+// then not taken and the int32 sweep runs.
+constexpr uint32_t kPStageTx = (uint32_t)kPStageWords * 4;  // bytes per stage
+constexpr int kMbarSpins = 1 << 20;
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// true once the phase with this parity has completed; false after the bound
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t addr = smem_u32(bar);
+    for (int i = 0; i < kMbarSpins; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // One tile (r0, w0) of D16 (row r0, word column w0) updated with the 256
-// pivots of the panels in colD / rowP.
+// pivots of the panels behind mapA (colD) and mapB (rowP).
 __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_t ld16, int64_t r0, int64_t w0,
-                                              const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP,
+                                              const CUtensorMap* mapA, const CUtensorMap* mapB, P16Status* st,
                                               int one) {
     extern __shared__ __align__(128) uint32_t psm[];
+    __shared__ __align__(8) uint64_t bars[kPStages];
+    __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
     const int64_t ldw = ld16 / 2;
+    constexpr int nslab = kPT / kSlab;
+    if (tid == 0) {
+        // TMA destinations must be 128-byte aligned; the stage sizes keep every
+        // stage and operand aligned when the base is.
+        s_ok = (smem_u32(psm) & 127u) == 0;
+        if (!s_ok) atomicOr(&st->copy_fault, 2u);
+        for (int i = 0; i < kPStages; ++i) mbar_init(&bars[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const bool ok = s_ok != 0;
+    auto issue = [&](int j) {  // slab j into stage j % kPStages, thread 0 only
+        if (tid == 0 && ok) {
+            const int stg = j % kPStages;
+            uint32_t* dst = psm + stg * kPStageWords;
+            mbar_expect_tx(&bars[stg], kPStageTx);
+            tma_load_2d(dst, mapA, (int)r0, j * kSlab, &bars[stg]);
+            tma_load_2d(dst + kPSlabA, mapB, (int)w0, j * kSlab, &bars[stg]);
+        }
+    };
     uint32_t c[8][8];
     p_load_tile(c, D16, ldw, r0, w0, tx, ty);
-    p_mainloop(
-        c, kPT / kSlab, psm, [&](uint32_t* dst, int s) { p_load_kmajor<kPT>(dst, colD, ld16, s * kSlab, r0, tid); },
-        [&](uint32_t* dst, int s) { p_load_kmajor<kPW>(dst, rowP, ldw, s * kSlab, w0, tid); }, tx, ty, one);
+#pragma unroll
+    for (int j = 0; j < kPStages - 1; ++j) issue(j);
+    bool arrived = true;
+    for (int kb = 0; kb < nslab; ++kb) {
+        const int stg = kb % kPStages;
+        if (ok && !mbar_wait(&bars[stg], (uint32_t)((kb / kPStages) & 1))) {
+            arrived = false;
+            atomicOr(&st->copy_fault, 1u);
+        }
+        __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
+        if (kb + kPStages - 1 < nslab) issue(kb + kPStages - 1);
+        if (ok && arrived) {
+            const uint32_t* stage = psm + stg * kPStageWords;
+            p_relax_slab<kP16MixA>(c, stage, stage + kPSlabA, tx, ty, one);
+        }
+    }
     p_store_tile(c, D16, ldw, r0, w0, tx, ty);
 }
 
@@ -426,19 +508,20 @@ __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_
 // the panels in colD / rowP.
 __global__ void __launch_bounds__(kPThreads, 1)
     fw_p16_remainder_kernel(uint16_t* __restrict__ D16, int64_t ld16, TileSet rows, TileSet cols,
-                            const uint32_t* __restrict__ colD, const uint32_t* __restrict__ rowP, const P16Status* st,
-                            int one) {
+                            const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                            P16Status* st, int one) {
     if (st->ineligible) return;
-    p_update_tile(D16, ld16, (int64_t)tile_of(rows, blockIdx.y) * kPT, (int64_t)tile_of(cols, blockIdx.x) * kPW, colD,
-                  rowP, one);
+    p_update_tile(D16, ld16, (int64_t)tile_of(rows, blockIdx.y) * kPT, (int64_t)tile_of(cols, blockIdx.x) * kPW,
+                  &mapA, &mapB, st, one);
 }
 
 // Block t's update of block u = t + 1's row and column in one launch: CTAs
 // [0, T - 1) take the row tiles (u, J), J != t; CTAs [T - 1, 2T - 3) the
 // column tiles (I, u), I != t, u.
 __global__ void __launch_bounds__(kPThreads, 1)
-    fw_p16_cross_kernel(uint16_t* __restrict__ D16, int64_t ld16, int t, int T, const uint32_t* __restrict__ colD,
-                        const uint32_t* __restrict__ rowP, const P16Status* st, int one) {
+    fw_p16_cross_kernel(uint16_t* __restrict__ D16, int64_t ld16, int t, int T,
+                        const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                        P16Status* st, int one) {
     if (st->ineligible) return;
     const int u = t + 1;
     int I, J;
@@ -449,10 +532,44 @@ __global__ void __launch_bounds__(kPThreads, 1)
         I = tile_of(all_but(t, u), blockIdx.x - (T - 1));
         J = u;
     }
-    p_update_tile(D16, ld16, (int64_t)I * kPT, (int64_t)J * kPW, colD, rowP, one);
+    p_update_tile(D16, ld16, (int64_t)I * kPT, (int64_t)J * kPW, &mapA, &mapB, st, one);
 }
 
 }  // namespace
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link libcuda itself).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// 2-D map over a k-major panel of `rows` rows of `width` 32-bit words
+// (16-byte aligned base, row stride width * 4 bytes), boxes of box_w x 32.
+int panel_map(CUtensorMap* map, const uint32_t* base, uint64_t width, uint64_t rows, uint32_t box_w) {
+    const auto fn = tensor_map_encoder();
+    if (!fn) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[2] = {width, rows};
+    const cuuint64_t strides[1] = {width * 4};
+    const cuuint32_t box[2] = {box_w, (cuuint32_t)kSlab};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint32_t*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return FW_OK;
+}
 
 int64_t p16_ld(int64_t n) { return (n + kPT - 1) / kPT * kPT; }
 
@@ -490,6 +607,13 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
     rowP[0] = colD[0] + (size_t)kPT * ld;
     colD[1] = rowP[0] + (size_t)kPT * (ld / 2);
     rowP[1] = colD[1] + (size_t)kPT * ld;
+    // TMA maps of the two panel buffers: colD rows of ld words (boxes of 256),
+    // rowP rows of ld / 2 words (boxes of 128).
+    CUtensorMap mapA[2], mapB[2];
+    for (int b = 0; b < 2; ++b) {
+        if (int rc = panel_map(&mapA[b], colD[b], (uint64_t)ld, kPT, kPT)) return rc;
+        if (int rc = panel_map(&mapB[b], rowP[b], (uint64_t)(ld / 2), kPT, kPW)) return rc;
+    }
     FW_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(P16Status), s));
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -524,8 +648,8 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
         if (nrows <= 0 || ncols <= 0) return FW_OK;
         const int b = t & 1;
         prof_begin(KC_P16_REMAINDER, q);
-        fw_p16_remainder_kernel<<<dim3(ncols, nrows), kPThreads, kPSmemBytes, q>>>(D16, ld, rows, cols, colD[b],
-                                                                                  rowP[b], st, 1);
+        fw_p16_remainder_kernel<<<dim3(ncols, nrows), kPThreads, kPSmemBytes, q>>>(D16, ld, rows, cols, mapA[b],
+                                                                                  mapB[b], st, 1);
         FW_LAUNCH_CHECK("fw_p16_remainder_kernel");
         prof_end(KC_P16_REMAINDER, q, rows_of(rows) * rows_of(cols) * kv(t));
         return FW_OK;
@@ -535,7 +659,7 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
     auto cross = [&](int t, cudaStream_t q) -> int {
         const int b = t & 1, u = t + 1;
         prof_begin(KC_P16_REMAINDER, q);
-        fw_p16_cross_kernel<<<(unsigned)(2 * T - 3), kPThreads, kPSmemBytes, q>>>(D16, ld, t, T, colD[b], rowP[b], st,
+        fw_p16_cross_kernel<<<(unsigned)(2 * T - 3), kPThreads, kPSmemBytes, q>>>(D16, ld, t, T, mapA[b], mapB[b], st,
                                                                                  1);
         FW_LAUNCH_CHECK("fw_p16_cross_kernel");
         prof_end(KC_P16_REMAINDER, q, (kv(u) * ((double)n - kv(t)) + ((double)n - kv(t) - kv(u)) * kv(u)) * kv(t));
