@@ -57,6 +57,7 @@ EXPORTED_SYMBOLS = (
     "fw_apsp_i32_host",
     "fw_generate_graph_device_i32",
     "fw_mt19937_outputs",
+    "fw_copy_faults",
     "fw_host_solve_device_bytes",
     "fw_batch_pack_offsets",
     "fw_batch_plan_create",
@@ -133,6 +134,8 @@ def lib():
     L.fw_generate_graph_device_i32.restype = c_int
     L.fw_mt19937_outputs.argtypes = [ctypes.c_uint32, ctypes.c_uint64, i64, vp]
     L.fw_mt19937_outputs.restype = c_int
+    L.fw_copy_faults.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    L.fw_copy_faults.restype = c_int
     L.fw_apsp_i32_host.argtypes = [vp, i64, i64, i64, vp]
     L.fw_apsp_i32_host.restype = c_int
     L.fw_host_solve_device_bytes.argtypes = [i64, i64, i64]
@@ -226,6 +229,13 @@ def mt19937_outputs(seed: int, skip: int, count: int) -> np.ndarray:
     out = np.empty(count, dtype=np.uint32)
     _check(lib().fw_mt19937_outputs(seed, skip, count, out.ctypes.data))
     return out
+
+
+def copy_faults() -> int:
+    """Remainder-kernel tile copies that missed their bounded wait (0 when healthy)."""
+    c = ctypes.c_uint(0)
+    _check(lib().fw_copy_faults(ctypes.byref(c)))
+    return int(c.value)
 
 
 def version() -> str:

@@ -35,8 +35,14 @@
 #include "fw_common.cuh"
 #include "fw_internal.h"
 #include "fw_tile.cuh"
+#include "fw_tma.cuh"
 
 namespace fw {
+
+// Tile copies that did not arrive within the bounded wait (a correct build
+// never counts one); read by fw_copy_faults.
+__device__ unsigned int g_copy_faults = 0;
+
 namespace {
 
 // ------------------------------------------------------------------ kernels
@@ -149,12 +155,28 @@ __global__ void __launch_bounds__(kThreads, 2)
 // the next nrows - 2 are (I, u), I != cross, u (nrows = T, ncols = 2T - 3).
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
-    fw_remainder_kernel(int* __restrict__ D, int64_t n, int64_t ldp, TileSet rows, int nrows, TileSet cols, int ncols,
-                        int slab0, int nslab, const int* __restrict__ colT, const int* __restrict__ rowP, int one,
-                        const unsigned* __restrict__ skip, int cross) {
+    fw_remainder_kernel(int* __restrict__ D, int64_t n, TileSet rows, int nrows, TileSet cols, int ncols, int slab0,
+                        int nslab, const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                        int one, const unsigned* __restrict__ skip, int cross) {
     if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
+    __shared__ __align__(8) uint64_t bars[kStages];
+    __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (tid == 0) {
+        // TMA destinations must be 128-byte aligned; the stage sizes keep every
+        // stage and operand aligned when the base is.
+        s_ok = (smem_u32(smem) & 127u) == 0;
+        if (!s_ok) atomicAdd(&g_copy_faults, 1u);
+        for (int i = 0; i < kStages; ++i) mbar_init(&bars[i], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const bool ok = s_ok != 0;
+    // Operand slabs, k-major 32 x 128 ints each, by TMA: slab j of the CTA's
+    // running count g + j goes to stage (g + j) % kStages, whose barrier
+    // completes for the ((g + j) / kStages)-th time.
+    int g = 0;
     const int64_t ntiles = cross >= 0 ? (int64_t)ncols : (int64_t)nrows * ncols;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int I, J;
@@ -168,13 +190,36 @@ __global__ void __launch_bounds__(kThreads, 2)
             I = tile_of(all_but(cross, cross + 1), (int)t - (nrows - 1));
             J = cross + 1;
         }
-        const int64_t r0 = (int64_t)I * kTile, c0 = (int64_t)J * kTile;
+        const int r0 = I * kTile, c0 = J * kTile;
+        auto issue = [&](int j) {
+            if (tid == 0 && ok) {
+                const int stg = (g + j) % kStages;
+                int* dst = smem + stg * kStageInts;
+                mbar_expect_tx(&bars[stg], (uint32_t)kStageInts * 4);
+                tma_load_2d(dst, &mapA, r0, (slab0 + j) * kSlab, &bars[stg]);
+                tma_load_2d(dst + kSlabInts, &mapB, c0, (slab0 + j) * kSlab, &bars[stg]);
+            }
+        };
         int acc[8][8];
         load_acc<VEC>(acc, D, n, r0, c0, tx, ty);
-        mainloop<kMixA>(
-            acc, nslab, smem,
-            [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, (slab0 + s) * kSlab, r0, tid); },
-            [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, (slab0 + s) * kSlab, c0, tid); }, tx, ty, one);
+#pragma unroll
+        for (int j = 0; j < kStages - 1; ++j)
+            if (j < nslab) issue(j);
+        bool arrived = true;
+        for (int kb = 0; kb < nslab; ++kb) {
+            const int stg = (g + kb) % kStages;
+            if (ok && !mbar_wait(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
+                if (arrived) atomicAdd(&g_copy_faults, 1u);
+                arrived = false;
+            }
+            __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
+            if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
+            if (ok && arrived) {
+                const int* st = smem + stg * kStageInts;
+                relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
+            }
+        }
+        g += nslab;
         store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
         __syncthreads();  // the next tile's prologue refills the ring
     }
@@ -271,6 +316,7 @@ struct Blocked {
     const unsigned* skip;
     int64_t resident_ctas = 304;  // CTAs of the persistent remainder: 2 per SM
     AuxStream aux{};
+    CUtensorMap mapA{}, mapB{};   // TMA maps over colT and rowP (all panel rows of the workspace)
 
     int64_t p0(int t) const { return (int64_t)t * kTile; }
     int64_t kv(int t) const { return n - p0(t) < kTile ? n - p0(t) : kTile; }
@@ -307,8 +353,8 @@ struct Blocked {
         const int64_t ntiles = cross >= 0 ? (int64_t)ncols : (int64_t)nrows * ncols;
         const unsigned grid = (unsigned)((skip && ntiles > resident_ctas) ? resident_ctas : ntiles);
         prof_begin(KC_REMAINDER, q);
-        fw_remainder_kernel<VEC><<<grid, kThreads, kSmemBytes, q>>>(D, n, ldp, rows, nrows, cols, ncols, slab0, nslab,
-                                                                    colT, rowP, 1, skip, cross);
+        fw_remainder_kernel<VEC><<<grid, kThreads, kSmemBytes, q>>>(D, n, rows, nrows, cols, ncols, slab0, nslab, mapA,
+                                                                    mapB, 1, skip, cross);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
         const double relax = cross >= 0
                                  ? ((double)kv(cross + 1) * (double)(n - kv(cross)) +
@@ -405,7 +451,7 @@ struct Blocked {
 };
 
 template <bool VEC>
-int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahead, int* colT, int* rowP,
+int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahead, int* colT, int* rowP, int sets,
                        cudaStream_t s, const unsigned* skip) {
     static bool attr_done = false;
     if (!attr_done) {
@@ -422,6 +468,8 @@ int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahea
         FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         b.resident_ctas = 2 * (int64_t)(sms > 0 ? sms : 152);
     }
+    if (int rc = panel_map(&b.mapA, colT, (uint64_t)b.ldp, (uint64_t)sets * kTile, kTile)) return rc;
+    if (int rc = panel_map(&b.mapB, rowP, (uint64_t)b.ldp, (uint64_t)sets * kTile, kTile)) return rc;
     if (blocks_per_pass == 1 && lookahead && b.T > 2) return b.lookahead();
     for (int t = 0; t < b.T;) {
         if (blocks_per_pass == 2 && t + 1 < b.T) {
@@ -461,8 +509,8 @@ int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, size_t ws_bytes, 
     int* colT = static_cast<int*>(ws);
     int* rowP = colT + (size_t)sets * kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    return vec ? blocked_solve_impl<true>(D, n, blocks, two, colT, rowP, s, skip)
-               : blocked_solve_impl<false>(D, n, blocks, two, colT, rowP, s, skip);
+    return vec ? blocked_solve_impl<true>(D, n, blocks, two, colT, rowP, sets, s, skip)
+               : blocked_solve_impl<false>(D, n, blocks, two, colT, rowP, sets, s, skip);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }
@@ -494,3 +542,9 @@ int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
 }
 
 }  // namespace fw
+
+extern "C" int fw_copy_faults(unsigned int* count) {
+    if (count == nullptr) return fw::set_error(FW_ERR_INVALID_ARGUMENT, "fw_copy_faults: count is NULL");
+    FW_CUDA_TRY(cudaMemcpyFromSymbol(count, fw::g_copy_faults, sizeof(unsigned int)));
+    return FW_OK;
+}

@@ -40,6 +40,7 @@
 
 #include "fw_common.cuh"
 #include "fw_internal.h"
+#include "fw_tma.cuh"
 
 namespace fw {
 namespace {
@@ -419,38 +420,6 @@ __global__ void __launch_bounds__(kPThreads, 1)
 // bounded; a copy that does not arrive sets copy_fault, the packed result is
 // then not taken and the int32 sweep runs.
 constexpr uint32_t kPStageTx = (uint32_t)kPStageWords * 4;  // bytes per stage
-constexpr int kMbarSpins = 1 << 20;
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// true once the phase with this parity has completed; false after the bound
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    const uint32_t addr = smem_u32(bar);
-    for (int i = 0; i < kMbarSpins; ++i) {
-        uint32_t ok;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(ok)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // One tile (r0, w0) of D16 (row r0, word column w0) updated with the 256
 // pivots of the panels behind mapA (colD) and mapB (rowP).
@@ -469,8 +438,7 @@ __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_
         s_ok = (smem_u32(psm) & 127u) == 0;
         if (!s_ok) atomicOr(&st->copy_fault, 2u);
         for (int i = 0; i < kPStages; ++i) mbar_init(&bars[i], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_init_fence();
     }
     __syncthreads();
     const bool ok = s_ok != 0;
@@ -536,40 +504,6 @@ __global__ void __launch_bounds__(kPThreads, 1)
 }
 
 }  // namespace
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (the
-// library does not link libcuda itself).
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            cudaGetLastError();
-    });
-    return fn;
-}
-
-// 2-D map over a k-major panel of `rows` rows of `width` 32-bit words
-// (16-byte aligned base, row stride width * 4 bytes), boxes of box_w x 32.
-int panel_map(CUtensorMap* map, const uint32_t* base, uint64_t width, uint64_t rows, uint32_t box_w) {
-    const auto fn = tensor_map_encoder();
-    if (!fn) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t dims[2] = {width, rows};
-    const cuuint64_t strides[1] = {width * 4};
-    const cuuint32_t box[2] = {box_w, (cuuint32_t)kSlab};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint32_t*>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-    return FW_OK;
-}
 
 int64_t p16_ld(int64_t n) { return (n + kPT - 1) / kPT * kPT; }
 

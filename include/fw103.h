@@ -222,6 +222,12 @@ int fw_generate_graph_device_i32(int32_t* d_D, int64_t n, double density, uint32
  * `skip` outputs, computed by the same polynomial jump-ahead (no device). */
 int fw_mt19937_outputs(uint32_t seed, uint64_t skip, int64_t count, uint32_t* h_out);
 
+/* Tile copies (TMA) of the int32 remainder kernel that did not arrive within
+ * their bounded wait since the library was loaded on this device: 0 in a
+ * working build. The kernel records the fault instead of waiting forever; the
+ * affected tiles are then not updated. Synchronous (reads a device word). */
+int fw_copy_faults(unsigned int* count);
+
 /* Message of the last failure on this host thread ("" if none). */
 const char* fw_last_error_string(void);
 

@@ -213,3 +213,9 @@ def test_reference_gpu_kernels_agree(fw, cuda, oracle):
             oracle.refgpu_run("multi_layer_tiling_gpu", t.data_ptr(), n, kappa)
             bad = int(np.count_nonzero(t.cpu().numpy() != truth))
             print(f"reference multi_layer_tiling_gpu kappa={kappa} n={n}: {bad} entries differ from baseline_cpu")
+
+
+def test_no_tile_copy_faults(fw, cuda):
+    """The remainder kernels' TMA copies all arrived within their bounded
+    waits during the solves above (a fault would be recorded, not hung on)."""
+    assert fw.copy_faults() == 0
