@@ -345,7 +345,7 @@ def run_ours(args) -> None:
         roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, 512, peak_packed,
                                "measured live: register-only packed 16-bit DPX add-min kernel "
                                "(fw_measure_relax_peak_packed)", hbm_peak, "hbm_gbs" in peaks,
-                               traffic_at_16384=532.27e6 + 445.96e6)
+                               traffic_at_16384=537.49e6 + 444.44e6)
         if roofline:
             roofline["int32_dpx_only_peak"] = peak_dpx
     else:
@@ -356,7 +356,7 @@ def run_ours(args) -> None:
                                256, peak_mixed,
                                "measured live: register-only relaxation kernels (fw_measure_relax_peak), "
                                "best instruction mix", hbm_peak, "hbm_gbs" in peaks,
-                               traffic_at_16384=(1.11e9 + 983.25e6) if pair else None)
+                               traffic_at_16384=(1.11e9 + 983.25e6) if pair else (1.07e9 + 979.55e6))
         if roofline:
             roofline["dpx_only_peak"] = peak_dpx
             roofline["frac_of_dpx_only"] = roofline["achieved"] / peak_dpx
