@@ -28,8 +28,13 @@
 
 #include "fw_common.cuh"
 #include "fw_internal.h"
+#include "fw_tma.cuh"
 
 namespace fw {
+
+// Remainder tile copies that missed their bounded wait (see fw_copy_faults).
+__device__ unsigned int g_nh_copy_faults = 0;
+
 namespace {
 
 constexpr int kFThreads = 512;  // 16 row groups x 32 column groups
@@ -58,6 +63,8 @@ constexpr int kFStages = 2;
 constexpr int kFSlabInts = kSlab * kTile;
 constexpr int kFStageInts = 3 * kFSlabInts;  // A values, A next hops, B values
 constexpr int kFSmemBytes = kFStages * kFStageInts * 4;  // 96 KB
+constexpr int kFTStages = 3;                              // remainder: TMA ring
+constexpr int kFTSmemBytes = kFTStages * kFStageInts * 4;  // 144 KB
 
 // Thread (tx = t % 32, ty = t / 32) of a 128 x 128 tile owns rows
 // own_row(ty, r), r < 8, and columns tx*4 .. tx*4+3.
@@ -341,17 +348,24 @@ __global__ void __launch_bounds__(kFThreads, 1)
 // (I, u), I != pt, u.
 template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
-    fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int64_t ldp, int pt, int T,
-                           TileSet rows, TileSet cols, int ncols, int cross, const V* __restrict__ colTall,
-                           const int* __restrict__ colHall, const V* __restrict__ rowPall) {
+    fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int pt, int T, TileSet rows,
+                           TileSet cols, int ncols, int cross, const __grid_constant__ CUtensorMap mapCT,
+                           const __grid_constant__ CUtensorMap mapCH, const __grid_constant__ CUtensorMap mapRP) {
     extern __shared__ __align__(128) int smem[];
-    const int64_t gph = blockIdx.z;
-    V* D = Dall + gph * n * n;
-    int* nh = nhall + gph * n * n;
-    const V* colT = colTall + gph * kTile * ldp;
-    const int* colH = colHall + gph * kTile * ldp;
-    const V* rowP = rowPall + gph * kTile * ldp;
+    __shared__ __align__(8) uint64_t bars[kFTStages];
+    __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    if (tid == 0) {
+        s_ok = (smem_u32(smem) & 127u) == 0;
+        if (!s_ok) atomicAdd(&g_nh_copy_faults, 1u);
+        for (int i = 0; i < kFTStages; ++i) mbar_init(&bars[i], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const bool ok = s_ok != 0;
+    const int gph = (int)blockIdx.z;
+    V* D = Dall + (int64_t)gph * n * n;
+    int* nh = nhall + (int64_t)gph * n * n;
     const int x = (int)blockIdx.x;
     int ti, tj;
     if (cross < 0) {
@@ -364,18 +378,43 @@ __global__ void __launch_bounds__(kFThreads, 1)
         ti = tile_of(all_but(pt, pt + 1), x - (T - 1));
         tj = pt + 1;
     }
-    const int64_t p0 = (int64_t)pt * kTile, r0 = (int64_t)ti * kTile, c0 = (int64_t)tj * kTile;
+    const int64_t p0 = (int64_t)pt * kTile;
+    const int r0 = ti * kTile, c0 = tj * kTile;
     const int kv = (int)(n - p0 < kTile ? n - p0 : kTile);
+    const int nslab = (kv + kSlab - 1) / kSlab;
+    // Per slab: the column panel's values and next hops at rows r0.., the row
+    // panel's values at columns c0.., by TMA into one stage.
+    auto issue = [&](int j) {
+        if (tid == 0 && ok) {
+            const int stg = j % kFTStages;
+            int* dst = smem + stg * kFStageInts;
+            mbar_expect_tx(&bars[stg], (uint32_t)kFStageInts * 4);
+            tma_load_3d(dst, &mapCT, r0, j * kSlab, gph, &bars[stg]);
+            tma_load_3d(dst + kFSlabInts, &mapCH, r0, j * kSlab, gph, &bars[stg]);
+            tma_load_3d(dst + 2 * kFSlabInts, &mapRP, c0, j * kSlab, gph, &bars[stg]);
+        }
+    };
     V c[8][4];
     int h[8][4];
     f_load_tile(c, h, D, nh, n, r0, c0, tx, ty);
-    f_mainloop(
-        c, h, kv, smem,
-        [&](V* av, int* ah, int s) {
-            f_load_kmajor(av, colT, ldp, s * kSlab, r0, tid);
-            f_load_kmajor(ah, colH, ldp, s * kSlab, r0, tid);
-        },
-        [&](V* bv, int s) { f_load_kmajor(bv, rowP, ldp, s * kSlab, c0, tid); }, tx, ty);
+#pragma unroll
+    for (int j = 0; j < kFTStages - 1; ++j)
+        if (j < nslab) issue(j);
+    bool arrived = true;
+    for (int kb = 0; kb < nslab; ++kb) {
+        const int stg = kb % kFTStages;
+        if (ok && !mbar_wait(&bars[stg], (uint32_t)((kb / kFTStages) & 1))) {
+            if (arrived) atomicAdd(&g_nh_copy_faults, 1u);
+            arrived = false;
+        }
+        __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
+        if (kb + kFTStages - 1 < nslab) issue(kb + kFTStages - 1);
+        if (ok && arrived) {
+            const int* st = smem + stg * kFStageInts;
+            f_relax_slab<V>(c, h, reinterpret_cast<const V*>(st), st + kFSlabInts,
+                            reinterpret_cast<const V*>(st + 2 * kFSlabInts), min(kSlab, kv - kb * kSlab), tx, ty);
+        }
+    }
     f_store_tile(c, h, D, nh, n, r0, c0, tx, ty);
 }
 
@@ -443,7 +482,7 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
         FW_CUDA_TRY(
             cudaFuncSetAttribute(fw_nh_panel_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
         FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+            cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFTSmemBytes));
         attr_done = true;
     }
     AuxStream aux;
@@ -460,6 +499,13 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
         rowP[b] = reinterpret_cast<V*>(colH[b] + panel);
     }
     const unsigned nb = (unsigned)batch;
+    // TMA maps over the panel buffers: batch panels of 128 rows x ldp each.
+    CUtensorMap mapCT[2], mapCH[2], mapRP[2];
+    for (int b = 0; b < 2; ++b) {
+        if (int rc = panel_map_3d(&mapCT[b], colT[b], (uint64_t)ldp, kTile, (uint64_t)batch, kTile)) return rc;
+        if (int rc = panel_map_3d(&mapCH[b], colH[b], (uint64_t)ldp, kTile, (uint64_t)batch, kTile)) return rc;
+        if (int rc = panel_map_3d(&mapRP[b], rowP[b], (uint64_t)ldp, kTile, (uint64_t)batch, kTile)) return rc;
+    }
     auto close = [&](int t, cudaStream_t q) -> int {
         const int b = t & 1;
         fw_nh_diag_kernel<V><<<dim3(1, 1, nb), kFThreads, 0, q>>>(D, nh, n, ldp, (int64_t)t * kTile, colT[b], colH[b],
@@ -476,8 +522,8 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
         const int tiles = cross >= 0 ? 2 * T - 3 : nrows * ncols;
         if (tiles <= 0) return FW_OK;
         const int b = t & 1;
-        fw_nh_remainder_kernel<V><<<dim3((unsigned)tiles, 1, nb), kFThreads, kFSmemBytes, q>>>(
-            D, nh, n, ldp, t, T, rows, cols, ncols, cross, colT[b], colH[b], rowP[b]);
+        fw_nh_remainder_kernel<V><<<dim3((unsigned)tiles, 1, nb), kFThreads, kFTSmemBytes, q>>>(
+            D, nh, n, t, T, rows, cols, ncols, cross, mapCT[b], mapCH[b], mapRP[b]);
         FW_LAUNCH_CHECK("fw_nh_remainder_kernel");
         return FW_OK;
     };
@@ -534,4 +580,12 @@ int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t ba
     return FW_OK;
 }
 
+}  // namespace fw
+
+namespace fw {
+unsigned int nh_copy_faults() {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_nh_copy_faults, sizeof(v)) != cudaSuccess) cudaGetLastError();
+    return v;
+}
 }  // namespace fw

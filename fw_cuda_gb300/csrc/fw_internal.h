@@ -99,6 +99,10 @@ int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t ba
 // int32 sweep that also records next hops (same kernels as the fp32 form).
 int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
 
+// Remainder tile copies of the next-hop forward that missed their bounded
+// wait (fw_diff.cu; part of fw_copy_faults).
+unsigned int nh_copy_faults();
+
 // Out-of-core sweep over a host-resident matrix (fw_ooc.cu); W and H are
 // validated multiples of 128.
 size_t ooc_device_bytes(int64_t n, int64_t W, int64_t H);

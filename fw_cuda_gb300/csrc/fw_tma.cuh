@@ -60,6 +60,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// 3-D form: box (x, y, z).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the
 // library does not link libcuda itself).
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -91,6 +100,25 @@ inline int panel_map(CUtensorMap* map, const void* base, uint64_t width, uint64_
     const cuuint32_t box[2] = {box_w, (cuuint32_t)kSlab};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return FW_OK;
+}
+
+// 3-D map over `depth` k-major panels of `rows` x `width` 32-bit elements
+// stored one after another, in boxes of box_w x kSlab x 1.
+inline int panel_map_3d(CUtensorMap* map, const void* base, uint64_t width, uint64_t rows, uint64_t depth,
+                        uint32_t box_w) {
+    const auto fn = tensor_map_encoder();
+    if (!fn) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (width * 4) % 16 != 0)
+        return set_error(FW_ERR_INTERNAL, "panel_map_3d: base or row stride not 16-byte aligned");
+    const cuuint64_t dims[3] = {width, rows, depth};
+    const cuuint64_t strides[2] = {width * 4, width * rows * 4};
+    const cuuint32_t box[3] = {box_w, (cuuint32_t)kSlab, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(base), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
