@@ -546,6 +546,6 @@ int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
 extern "C" int fw_copy_faults(unsigned int* count) {
     if (count == nullptr) return fw::set_error(FW_ERR_INVALID_ARGUMENT, "fw_copy_faults: count is NULL");
     FW_CUDA_TRY(cudaMemcpyFromSymbol(count, fw::g_copy_faults, sizeof(unsigned int)));
-    *count += fw::nh_copy_faults();
+    *count += fw::nh_copy_faults() + fw::ooc_copy_faults();
     return FW_OK;
 }

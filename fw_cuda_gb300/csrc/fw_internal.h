@@ -102,6 +102,8 @@ int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t 
 // Remainder tile copies of the next-hop forward that missed their bounded
 // wait (fw_diff.cu; part of fw_copy_faults).
 unsigned int nh_copy_faults();
+// The same for the out-of-core update kernel (fw_ooc.cu).
+unsigned int ooc_copy_faults();
 
 // Out-of-core sweep over a host-resident matrix (fw_ooc.cu); W and H are
 // validated multiples of 128.

@@ -31,8 +31,13 @@
 #include "fw_common.cuh"
 #include "fw_internal.h"
 #include "fw_tile.cuh"
+#include "fw_tma.cuh"
 
 namespace fw {
+
+// Update-kernel tile copies that missed their bounded wait (see fw_copy_faults).
+__device__ unsigned int g_ooc_copy_faults = 0;
+
 namespace {
 
 __global__ void fw_ooc_fill_kernel(int* __restrict__ p, int64_t count) {
@@ -113,26 +118,62 @@ __device__ __forceinline__ int64_t skip_gap(int64_t idx, const TileGap& g) { ret
 
 // C[i][j] = min(C[i][j], min_k A[k][i] + B[k][j]) for i < M, j < N and
 // k < 32 * nslab, over the 128 x 128 tiles outside the row gap and the column
-// gap. A and B are k-major with leading dimensions that are multiples of 4
-// and cover whole 128-wide tiles (INF where there is no value), as are their
-// 32-row slabs. Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x,
-// ... The main loop is the in-core remainder's.
+// gap. A and B are k-major panels behind 2-D tensor maps whose extents cover
+// whole 128-wide tiles (INF where there is no value); their 32-row slabs
+// arrive by TMA into the 3-stage ring, one mbarrier per stage, the stage and
+// parity count running across the tiles a persistent CTA takes. The main loop
+// is the in-core remainder's.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
-    fw_ooc_update_kernel(int* __restrict__ C, int64_t ldc, int64_t M, int64_t N, const int* __restrict__ A,
-                         int64_t lda, const int* __restrict__ B, int64_t ldb, int nslab, TileGap rgap, TileGap cgap,
-                         int one) {
+    fw_ooc_update_kernel(int* __restrict__ C, int64_t ldc, int64_t M, int64_t N,
+                         const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nslab,
+                         TileGap rgap, TileGap cgap, int one) {
     extern __shared__ __align__(128) int smem[];
+    __shared__ __align__(8) uint64_t bars[kStages];
+    __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (tid == 0) {
+        s_ok = (smem_u32(smem) & 127u) == 0;
+        if (!s_ok) atomicAdd(&g_ooc_copy_faults, 1u);
+        for (int i = 0; i < kStages; ++i) mbar_init(&bars[i], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    const bool ok = s_ok != 0;
+    int g = 0;
     const int64_t tn = (N + kTile - 1) / kTile - (cgap.x1 - cgap.x0);
     const int64_t ntiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * tn;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t r0 = skip_gap(t / tn, rgap) * kTile, c0 = skip_gap(t % tn, cgap) * kTile;
+        auto issue = [&](int j) {
+            if (tid == 0 && ok) {
+                const int stg = (g + j) % kStages;
+                int* dst = smem + stg * kStageInts;
+                mbar_expect_tx(&bars[stg], (uint32_t)kStageInts * 4);
+                tma_load_2d(dst, &mapA, (int)r0, j * kSlab, &bars[stg]);
+                tma_load_2d(dst + kSlabInts, &mapB, (int)c0, j * kSlab, &bars[stg]);
+            }
+        };
         int acc[8][8];
         ooc_load_acc<VEC>(acc, C, ldc, M, N, r0, c0, tx, ty);
-        mainloop<kMixA>(
-            acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, A, lda, s * kSlab, r0, tid); },
-            [&](int* dst, int s) { load_kmajor_async(dst, B, ldb, s * kSlab, c0, tid); }, tx, ty, one);
+#pragma unroll
+        for (int j = 0; j < kStages - 1; ++j)
+            if (j < nslab) issue(j);
+        bool arrived = true;
+        for (int kb = 0; kb < nslab; ++kb) {
+            const int stg = (g + kb) % kStages;
+            if (ok && !mbar_wait(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
+                if (arrived) atomicAdd(&g_ooc_copy_faults, 1u);
+                arrived = false;
+            }
+            __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
+            if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
+            if (ok && arrived) {
+                const int* st = smem + stg * kStageInts;
+                relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
+            }
+        }
+        g += nslab;
         ooc_store_acc<VEC>(acc, C, ldc, M, N, r0, c0, tx, ty);
         __syncthreads();  // the next tile's prologue refills the ring
     }
@@ -191,21 +232,27 @@ int transpose(const int* src, int64_t lds, int* dst, int64_t ldd, int64_t rows, 
     return FW_OK;
 }
 
-int update(int* C, int64_t ldc, int64_t M, int64_t N, const int* A, int64_t lda, const int* B, int64_t ldb,
-           int64_t kvalid, int64_t resident, cudaStream_t s, TileGap rgap = {0, 0}, TileGap cgap = {0, 0}) {
+// A: k-major panel of panel_rows rows, leading dimension lda, of which the
+// a_cols columns from A are valid addresses (the same for B).
+int update(int* C, int64_t ldc, int64_t M, int64_t N, const int* A, int64_t lda, int64_t a_cols, const int* B,
+           int64_t ldb, int64_t b_cols, int64_t panel_rows, int64_t kvalid, int64_t resident, cudaStream_t s,
+           TileGap rgap = {0, 0}, TileGap cgap = {0, 0}) {
     const int64_t tiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * ((N + kTile - 1) / kTile - (cgap.x1 - cgap.x0));
     if (tiles <= 0) return FW_OK;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, resident);
     const int nslab = (int)((kvalid + kSlab - 1) / kSlab);
     // 16-byte accesses need aligned rows and whole vectors inside [0, N).
     const bool vec = (ldc % 4) == 0 && (N % 4) == 0 && (reinterpret_cast<uintptr_t>(C) & 15u) == 0;
+    CUtensorMap mapA, mapB;
+    if (int rc = panel_map_ld(&mapA, A, (uint64_t)a_cols, (uint64_t)lda, (uint64_t)panel_rows, kTile)) return rc;
+    if (int rc = panel_map_ld(&mapB, B, (uint64_t)b_cols, (uint64_t)ldb, (uint64_t)panel_rows, kTile)) return rc;
     prof_begin(KC_OOC_UPDATE, s);
     if (vec)
         fw_ooc_update_kernel<true>
-            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, rgap, cgap, 1);
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1);
     else
         fw_ooc_update_kernel<false>
-            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, A, lda, B, ldb, nslab, rgap, cgap, 1);
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1);
     FW_LAUNCH_CHECK("fw_ooc_update_kernel");
     const double rows = (double)M - std::min<double>((double)M, (double)(rgap.x1 - rgap.x0) * kTile);
     const double cols = (double)N - std::min<double>((double)N, (double)(cgap.x1 - cgap.x0) * kTile);
@@ -312,8 +359,8 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
         // Panels: R2 = min(R, Dg* (x) R), CT2 = min(CT, Dg*^T (x) CT).
         FW_CUDA_TRY(cudaMemcpyAsync(st.R2, st.R, sizeof(int) * Wp * ldp, cudaMemcpyDeviceToDevice, s));
         FW_CUDA_TRY(cudaMemcpyAsync(st.CT2, st.CT, sizeof(int) * Wp * ldp, cudaMemcpyDeviceToDevice, s));
-        if (int rc = update(st.R2, ldp, w, n, st.DgT, Wp, st.R, ldp, w, resident, s)) return rc;
-        if (int rc = update(st.CT2, ldp, w, n, st.DgK, Wp, st.CT, ldp, w, resident, s)) return rc;
+        if (int rc = update(st.R2, ldp, w, n, st.DgT, Wp, Wp, st.R, ldp, ldp, Wp, w, resident, s)) return rc;
+        if (int rc = update(st.CT2, ldp, w, n, st.DgK, Wp, Wp, st.CT, ldp, ldp, Wp, w, resident, s)) return rc;
         FW_CUDA_TRY(cudaEventRecord(st.ev_panels, s));
         // Stripes.
         for (int64_t r0 = 0; r0 < n; r0 += H, ++stripe_no) {
@@ -329,7 +376,8 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
             const int64_t pr0 = std::max(p0, r0), pr1 = std::min(p0 + w, r0 + h);  // P rows in the stripe
             const TileGap rgap = pr0 < pr1 ? TileGap{(pr0 - r0) / kTile, (pr1 - r0 + kTile - 1) / kTile} : TileGap{0, 0};
             const TileGap cgap{p0 / kTile, (p0 + w + kTile - 1) / kTile};
-            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, st.R2, ldp, w, resident, s, rgap, cgap))
+            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, ldp - r0, st.R2, ldp, ldp, Wp, w, resident, s,
+                                rgap, cgap))
                 return rc;
             // columns of P: the column panel, transposed back
             if (int rc = transpose(st.CT2 + r0, ldp, st.buf[b] + p0, n, w, h, s)) return rc;
@@ -409,3 +457,11 @@ int fw_apsp_i32_host(int32_t* h_D, int64_t n, int64_t pass_width, int64_t stripe
 }
 
 }  // extern "C"
+
+namespace fw {
+unsigned int ooc_copy_faults() {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_ooc_copy_faults, sizeof(v)) != cudaSuccess) cudaGetLastError();
+    return v;
+}
+}  // namespace fw

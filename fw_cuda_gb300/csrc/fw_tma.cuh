@@ -106,6 +106,25 @@ inline int panel_map(CUtensorMap* map, const void* base, uint64_t width, uint64_
     return FW_OK;
 }
 
+// 2-D map over `rows` rows of `width` 32-bit elements with leading dimension
+// ld (elements; ld * 4 a multiple of 16), in boxes of box_w x kSlab.
+inline int panel_map_ld(CUtensorMap* map, const void* base, uint64_t width, uint64_t ld, uint64_t rows,
+                        uint32_t box_w) {
+    const auto fn = tensor_map_encoder();
+    if (!fn) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (ld * 4) % 16 != 0 || width > ld)
+        return set_error(FW_ERR_INTERNAL, "panel_map_ld: base, leading dimension or width not valid");
+    const cuuint64_t dims[2] = {width, rows};
+    const cuuint64_t strides[1] = {ld * 4};
+    const cuuint32_t box[2] = {box_w, (cuuint32_t)kSlab};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(FW_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return FW_OK;
+}
+
 // 3-D map over `depth` k-major panels of `rows` x `width` 32-bit elements
 // stored one after another, in boxes of box_w x kSlab x 1.
 inline int panel_map_3d(CUtensorMap* map, const void* base, uint64_t width, uint64_t rows, uint64_t depth,
