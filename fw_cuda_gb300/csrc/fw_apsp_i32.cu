@@ -15,10 +15,10 @@
 // The panels are also written to a workspace in the layout the remainder
 // reads: the column panel transposed (colT[k][i] = D[i][p0 + k]) and the row
 // panel as is (rowP[k][j] = D[p0 + k][j]), both with a leading dimension
-// padded to a multiple of 128. Every remainder operand slab is then a
-// contiguous, 16-byte aligned 32 x 128 block that streams into shared memory
-// with cp.async, and the remainder never reads a value another CTA of the
-// same launch writes.
+// padded to a multiple of 128. Every remainder operand slab is then one
+// 32 x 128 box of a 2-D tensor map that the tensor memory accelerator copies
+// into shared memory, and the remainder never reads a value another CTA of
+// the same launch writes.
 //
 // With integer weights and no negative cycle every stored value is an exact
 // path length below INF or INF itself, so the result does not depend on the

@@ -12,7 +12,8 @@
 // (blockIdx.z = graph). Tiles are 128 x 128 on 512-thread CTAs (an 8 x 4
 // value + next-hop register micro-tile per thread); the remainder streams a
 // value slab and a next-hop slab of the transposed column panel plus a value
-// slab of the row panel per 32 pivots through a two-stage cp.async ring.
+// slab of the row panel per 32 pivots, copied by TMA into a three-stage ring
+// (the panels use a two-stage cp.async ring).
 //
 // Backward, per graph and destination j: the next hops toward j form a tree
 // rooted at j, and edge (u, nh[u][j]) lies on the path i -> j exactly when u

@@ -137,6 +137,8 @@ __device__ __forceinline__ void store_acc_ws_transposed(const int (&acc)[8][8], 
 }
 
 // Multi-stage cp.async pipeline over `nslab` operand slabs: acc = min(acc, A (x) B).
+// (The panel kernels and the batched kernel use it; the remainder kernels
+// stream their slabs by TMA instead.)
 // la(dst, s) / lb(dst, s) fill slab s of A / B (asynchronously or not).
 template <int MIXA, class LA, class LB>
 __device__ __forceinline__ void mainloop(int (&acc)[8][8], int nslab, int* smem, LA la, LB lb, int tx, int ty,
