@@ -1,0 +1,59 @@
+"""Host-side checks of bench.py: the reference arm's JSON line (it runs on the
+host cores, so it runs here), the roofline arithmetic, and the clock-sample
+summary that decides whether a run saw throttling."""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def test_reference_arm_line():
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "128",
+                          "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["n_gpus"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "baseline_cpu" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # without a GPU the reference's own kernels cannot run; the line says why
+    assert "reference_gpu" in d
+
+
+def test_roofline_arithmetic():
+    n = 8192
+    stats = {"launches": 4, "total_ms": 2.0, "relaxations": 4 * (n - 512) ** 2 * 256.0}
+    r = bench.roofline_of(stats, "k", n, 256, 2, 512, 4.0e13, "probe", 6790.0, True, traffic_at_16384=1e9)
+    achieved = stats["relaxations"] / 2e-3
+    assert r["achieved"] == pytest.approx(achieved) and r["frac"] == pytest.approx(achieved / 4.0e13)
+    # tile bytes: each entry read and written once per launch of 256 pivots, 2 bytes per value
+    assert r["hbm"]["achieved"] == pytest.approx(stats["relaxations"] * 4 / 256 / 2e-3 / 1e9)
+    assert r["bulk_launch"]["algorithmic_bytes"] == 4.0 * (n - 512) ** 2
+    assert r["traffic"] == pytest.approx(1e9 * ((n - 512) / (16384 - 512)) ** 2)
+    assert bench.roofline_of(None, "k", n, 256, 2, 512, 1.0, "", 1.0, True) is None
+
+
+def test_clock_summary_flags_throttling():
+    s = bench.ClockSampler(0)
+    s.lines = [
+        "0, 2070, 2070, 400.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2065, 2070, 420.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 1800, 2070, 430.0, 0x8, Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    r = s.summary()
+    assert r["samples"] == 3 and r["sm_max_mhz"] == 2070.0 and r["sm_mhz"] == 2065.0 and r["sm_mhz_min"] == 1800.0
+    assert r["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert bench.ClockSampler(0).summary()["samples"] == 0
