@@ -70,26 +70,21 @@ __device__ __forceinline__ int prow_of(int ty, int r) { return (r < 4) ? ty * 4 
 __device__ __forceinline__ int pword_of(int tx, int w) { return (w < 4) ? tx * 4 + w : 64 + tx * 4 + (w - 4); }
 
 // ------------------------------------------------------------ encode / decode
-__global__ void fw_p16_encode_kernel(const int* __restrict__ D, int64_t n, uint16_t* __restrict__ D16, int64_t ld16,
-                                     P16Status* st) {
-    unsigned bad = 0, wmax = 0;
-    const int64_t total = ld16 * ld16;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = q / ld16, j = q % ld16;
-        uint32_t e = kCap;
-        if (i < n && j < n) {
-            const int v = D[i * n + j];
-            if (v == kInf) {
-                e = kCap;
-            } else if (v >= 0 && (uint32_t)v < kCap) {
-                e = (uint32_t)v;
-                wmax = max(wmax, (unsigned)v);
-            } else {
-                bad = 1;
-            }
-        }
-        D16[q] = (uint16_t)e;
+// Row-parallel passes over the matrix, eight values per thread: one 16-byte
+// D16 vector, two 16-byte int32 vectors when n % 4 == 0 and the eight values
+// lie inside the row, single values otherwise. blockIdx.y strides over rows.
+constexpr int kCodeThreads = 256;
+__device__ __forceinline__ uint32_t encode1(int v, unsigned& bad, unsigned& wmax) {
+    if (v == kInf) return kCap;
+    if (v >= 0 && (uint32_t)v < kCap) {
+        wmax = max(wmax, (unsigned)v);
+        return (uint32_t)v;
     }
+    bad = 1;
+    return kCap;
+}
+
+__device__ __forceinline__ void reduce_status(unsigned bad, unsigned wmax, P16Status* st) {
     for (int o = 16; o > 0; o >>= 1) {
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
         wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
@@ -100,25 +95,81 @@ __global__ void fw_p16_encode_kernel(const int* __restrict__ D, int64_t n, uint1
     }
 }
 
-__global__ void fw_p16_rmax_kernel(const uint16_t* __restrict__ D16, int64_t n, int64_t ld16, P16Status* st) {
+template <bool VEC>
+__global__ void __launch_bounds__(kCodeThreads)
+    fw_p16_encode_kernel(const int* __restrict__ D, int64_t n, uint16_t* __restrict__ D16, int64_t ld16,
+                         P16Status* st) {
+    unsigned bad = 0, wmax = 0;
+    for (int64_t i = blockIdx.y; i < ld16; i += gridDim.y) {
+        for (int64_t j0 = ((int64_t)blockIdx.x * kCodeThreads + threadIdx.x) * 8; j0 < ld16;
+             j0 += (int64_t)gridDim.x * kCodeThreads * 8) {
+            uint32_t e[8];
+            if (VEC && i < n && j0 + 8 <= n) {
+                const int4 a = *reinterpret_cast<const int4*>(D + i * n + j0);
+                const int4 b = *reinterpret_cast<const int4*>(D + i * n + j0 + 4);
+                e[0] = encode1(a.x, bad, wmax); e[1] = encode1(a.y, bad, wmax);
+                e[2] = encode1(a.z, bad, wmax); e[3] = encode1(a.w, bad, wmax);
+                e[4] = encode1(b.x, bad, wmax); e[5] = encode1(b.y, bad, wmax);
+                e[6] = encode1(b.z, bad, wmax); e[7] = encode1(b.w, bad, wmax);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    e[u] = (i < n && j0 + u < n) ? encode1(D[i * n + j0 + u], bad, wmax) : kCap;
+            }
+            *reinterpret_cast<uint4*>(D16 + i * ld16 + j0) =
+                make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+        }
+    }
+    reduce_status(bad, wmax, st);
+}
+
+__global__ void __launch_bounds__(kCodeThreads)
+    fw_p16_rmax_kernel(const uint16_t* __restrict__ D16, int64_t n, int64_t ld16, P16Status* st) {
     if (st->ineligible || st->copy_fault) return;
     unsigned m = 0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = D16[(q / n) * ld16 + q % n];
-        if (v < kCap) m = max(m, v);
+    for (int64_t i = blockIdx.y; i < n; i += gridDim.y) {
+        for (int64_t j0 = ((int64_t)blockIdx.x * kCodeThreads + threadIdx.x) * 8; j0 < n;
+             j0 += (int64_t)gridDim.x * kCodeThreads * 8) {
+            const uint4 w = *reinterpret_cast<const uint4*>(D16 + i * ld16 + j0);
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t v = (ws[u >> 1] >> ((u & 1) * 16)) & 0xFFFFu;
+                if (j0 + u < n && v < kCap) m = max(m, v);
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m) atomicMax(&st->rmax, m);
 }
 
-__global__ void fw_p16_decode_kernel(const uint16_t* __restrict__ D16, int* __restrict__ D, int64_t n, int64_t ld16,
-                                     P16Status* st) {
+template <bool VEC>
+__global__ void __launch_bounds__(kCodeThreads)
+    fw_p16_decode_kernel(const uint16_t* __restrict__ D16, int* __restrict__ D, int64_t n, int64_t ld16,
+                         P16Status* st) {
     if (st->ineligible || st->copy_fault || st->rmax + st->wmax >= kCap) return;  // the int32 sweep runs instead
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n * n; q += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = D16[(q / n) * ld16 + q % n];
-        D[q] = (v == kCap) ? kInf : (int)v;
+    for (int64_t i = blockIdx.y; i < n; i += gridDim.y) {
+        for (int64_t j0 = ((int64_t)blockIdx.x * kCodeThreads + threadIdx.x) * 8; j0 < n;
+             j0 += (int64_t)gridDim.x * kCodeThreads * 8) {
+            const uint4 w = *reinterpret_cast<const uint4*>(D16 + i * ld16 + j0);
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+            int o[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t v = (ws[u >> 1] >> ((u & 1) * 16)) & 0xFFFFu;
+                o[u] = (v == kCap) ? kInf : (int)v;
+            }
+            if (VEC && j0 + 8 <= n) {
+                *reinterpret_cast<int4*>(D + i * n + j0) = make_int4(o[0], o[1], o[2], o[3]);
+                *reinterpret_cast<int4*>(D + i * n + j0 + 4) = make_int4(o[4], o[5], o[6], o[7]);
+            } else {
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (j0 + u < n) D[i * n + j0 + u] = o[u];
+            }
+        }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 1;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) st->done = 1;
 }
 
 // ------------------------------------------------------------ tile helpers
@@ -549,11 +600,15 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
         if (int rc = panel_map(&mapB[b], rowP[b], (uint64_t)(ld / 2), kPT, kPW)) return rc;
     }
     FW_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(P16Status), s));
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned grid = (unsigned)(sms > 0 ? sms * 8 : 1024);
-    fw_p16_encode_kernel<<<grid, 256, 0, s>>>(D, n, D16, ld, st);
+    // Encode / check / decode: column chunks of 2048 values across blockIdx.x,
+    // rows strided over blockIdx.y.
+    const bool vec = (n % 4) == 0;
+    const dim3 cgrid((unsigned)((ld + 8 * kCodeThreads - 1) / (8 * kCodeThreads)),
+                     (unsigned)(ld < 2048 ? ld : 2048));
+    if (vec)
+        fw_p16_encode_kernel<true><<<cgrid, kCodeThreads, 0, s>>>(D, n, D16, ld, st);
+    else
+        fw_p16_encode_kernel<false><<<cgrid, kCodeThreads, 0, s>>>(D, n, D16, ld, st);
     FW_LAUNCH_CHECK("fw_p16_encode_kernel");
 
     auto kv = [&](int t) { return (double)((n - (int64_t)t * kPT) < kPT ? n - (int64_t)t * kPT : kPT); };
@@ -628,9 +683,12 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
     }
     // The side stream's last launch follows every launch of the chain.
     FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.bulk[(T - 1) & 1], 0));
-    fw_p16_rmax_kernel<<<grid, 256, 0, s>>>(D16, n, ld, st);
+    fw_p16_rmax_kernel<<<cgrid, kCodeThreads, 0, s>>>(D16, n, ld, st);
     FW_LAUNCH_CHECK("fw_p16_rmax_kernel");
-    fw_p16_decode_kernel<<<grid, 256, 0, s>>>(D16, D, n, ld, st);
+    if (vec)
+        fw_p16_decode_kernel<true><<<cgrid, kCodeThreads, 0, s>>>(D16, D, n, ld, st);
+    else
+        fw_p16_decode_kernel<false><<<cgrid, kCodeThreads, 0, s>>>(D16, D, n, ld, st);
     FW_LAUNCH_CHECK("fw_p16_decode_kernel");
     *done_flag = &st->done;
     return FW_OK;
