@@ -48,8 +48,9 @@ def test_reference_default_weights(fw, cuda, oracle):
 
 
 def test_beyond_reference_max_n(fw, cuda, oracle):
-    """n = 40000 (6.4 GB): the out-of-core result equals the in-core one bit
-    for bit, and sampled rows equal the oracle's Dijkstra rows."""
+    """n = 40000 (6.4 GB): the out-of-core result equals the in-core int32
+    and packed results bit for bit, and sampled rows equal the oracle's
+    Dijkstra rows."""
     torch = cuda
     n = 40000
     g = torch.Generator(device="cuda").manual_seed(4242)
@@ -66,9 +67,14 @@ def test_beyond_reference_max_n(fw, cuda, oracle):
         W_rows[r] = oracle.sssp_row(W_host, r)
     del W_host
 
+    d_auto = d.clone()
     fw.apsp_i32(d, n, 32, 8, fw.VARIANT_MULTI_LAYER, None)
+    fw.apsp_i32(d_auto, n, 32, 8, fw.VARIANT_AUTO, None)
+    assert fw.auto_used_packed(None)
     fw.apsp_i32_host(h, n, 2048, 0)
     torch.cuda.synchronize()
+    assert torch.equal(d, d_auto)
+    del d_auto
     assert torch.equal(d.cpu(), h)
     out = h.numpy()
     for r in rows:
