@@ -140,7 +140,7 @@ def lib():
     L.fw_apsp_i32_host.restype = c_int
     L.fw_host_solve_device_bytes.argtypes = [i64, i64, i64]
     L.fw_host_solve_device_bytes.restype = ctypes.c_size_t
-    L.fw_measure_relax_peak_packed.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
+    L.fw_measure_relax_peak_packed.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), vp]
     L.fw_measure_relax_peak_packed.restype = c_int
     L.fw_apsp_auto_report.argtypes = [vp, ctypes.POINTER(c_int)]
     L.fw_apsp_auto_report.restype = c_int
@@ -267,11 +267,11 @@ def measure_relax_peak(stream=None) -> tuple[float, float]:
     return a.value, b.value
 
 
-def measure_relax_peak_packed(stream=None) -> float:
-    """Relaxations/s of the register-only packed 16-bit DPX kernel."""
-    a = ctypes.c_double(0)
-    _check(lib().fw_measure_relax_peak_packed(ctypes.byref(a), _stream(stream)))
-    return a.value
+def measure_relax_peak_packed(stream=None) -> tuple[float, float]:
+    """(DPX-only, best mixed) relaxations/s of the register-only packed 16-bit kernels."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    _check(lib().fw_measure_relax_peak_packed(ctypes.byref(a), ctypes.byref(b), _stream(stream)))
+    return a.value, b.value
 
 
 # ------------------------------------------------------ paths, graph I/O, checks

@@ -103,8 +103,12 @@ def build(verbose: bool = False) -> str:
         _run([nvcc(), *ARCH, "-o", tool, tool_obj, f"-L{LIBDIR}", "-lfw103", "-Xlinker", "-rpath,$ORIGIN"])
     for alias in TOOLS[1:]:
         ap = os.path.join(LIBDIR, alias)
-        if os.path.lexists(ap):
+        if os.path.islink(ap) and os.readlink(ap) == TOOLS[0]:
+            continue
+        try:
             os.remove(ap)
+        except FileNotFoundError:
+            pass
         os.symlink(TOOLS[0], ap)
     if verbose:
         print("built", lib)

@@ -375,8 +375,8 @@ int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream) {
     return measure_relax_peak(dpx_only, mixed, reinterpret_cast<cudaStream_t>(stream));
 }
 
-int fw_measure_relax_peak_packed(double* packed, fw_stream_t stream) {
-    return measure_relax_peak_packed(packed, reinterpret_cast<cudaStream_t>(stream));
+int fw_measure_relax_peak_packed(double* dpx_only, double* mixed, fw_stream_t stream) {
+    return measure_relax_peak_packed(dpx_only, mixed, reinterpret_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

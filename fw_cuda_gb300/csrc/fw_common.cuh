@@ -30,9 +30,10 @@ constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 
 // Number of the 8 micro-tile columns that fold a pivot pair with two DPX
 // add-min instructions; the other columns use form B (see relax2). Measured on
-// GB300 in the remainder kernel (one launch, n = 16384): 8 of 8 (DPX only)
-// 1.78e13, 3 of 8 1.83e13, 5 of 8 1.86e13, 0 of 8 1.54e13 relaxations/s.
-constexpr int kMixA = 5;
+// GB300 with the TMA-fed remainder kernel (whole multi-layer solve, kappa 8,
+// n = 32768): 8 of 8 (DPX only) 1975 ms, 7 of 8 1918, 6 of 8 1797, 5 of 8
+// 1806, 4 of 8 1807, 3 of 8 1715, 2 of 8 1846, 1 of 8 2045 ms.
+constexpr int kMixA = 3;
 
 // Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
 // ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns

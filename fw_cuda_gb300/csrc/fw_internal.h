@@ -112,6 +112,6 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s);
 
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);
-int measure_relax_peak_packed(double* packed, cudaStream_t s);
+int measure_relax_peak_packed(double* dpx_only, double* mixed, cudaStream_t s);
 
 }  // namespace fw

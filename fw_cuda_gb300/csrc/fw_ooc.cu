@@ -40,6 +40,9 @@ __device__ unsigned int g_ooc_copy_faults = 0;
 
 namespace {
 
+// Instruction mix of the stripe update (see kMixA).
+constexpr int kOocMixA = 5;
+
 __global__ void fw_ooc_fill_kernel(int* __restrict__ p, int64_t count) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = kInf;
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
             if (ok && arrived) {
                 const int* st = smem + stg * kStageInts;
-                relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
+                relax_slab<kOocMixA>(acc, st, st + kSlabInts, tx, ty, one);
             }
         }
         g += nslab;

@@ -245,10 +245,10 @@ __device__ __forceinline__ void p_load_transposed_dup(uint32_t* dst, const uint1
 // Number of the 8 word columns that fold a pivot pair with two packed DPX
 // add-mins; the others add with two 32-bit multiply-adds (exact as packed
 // adds: each half stays below 65535, so no carry crosses the halves) on the
-// FMA pipe and take one packed three-way DPX min. Measured on GB300 (one
-// remainder launch, n = 16384): 8 of 8 3.32e13, 6 of 8 3.60e13, 5 of 8
-// 3.46e13, 4 of 8 3.57e13, 3 of 8 3.41e13 relaxations/s.
-constexpr int kP16MixA = 6;
+// FMA pipe and take one packed three-way DPX min. Measured on GB300 with the
+// TMA-fed remainder kernel (whole packed solve, n = 32768): 7 of 8 964 ms,
+// 6 of 8 942, 5 of 8 922, 4 of 8 884, 3 of 8 930, 2 of 8 978 ms.
+constexpr int kP16MixA = 4;
 
 template <int MIXW>
 __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t* As, const uint32_t* Bs, int tx,

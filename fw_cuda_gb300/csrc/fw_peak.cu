@@ -48,22 +48,44 @@ __global__ void __launch_bounds__(256) fw_peak_kernel(const int* __restrict__ in
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-// Packed 16-bit DPX add-min: two relaxations per instruction, 16 accumulators
-// of two lanes each, operands from other accumulators.
-__global__ void __launch_bounds__(256) fw_peak_packed_kernel(const unsigned* __restrict__ in, unsigned* __restrict__ out,
-                                                             int iters) {
-    unsigned acc[16], a[4];
+// Packed 16-bit relaxations: 16 accumulator words of two 15-bit lanes each
+// fold pivot pairs exactly as the packed remainder kernel does (word columns
+// below MIXW: two packed DPX add-mins; the others: two adds on the FMA pipe and
+// one packed three-way DPX min), operands from other accumulators.
+template <int MIXW>
+__global__ void __launch_bounds__(256) fw_peak_packed_kernel(const unsigned* __restrict__ in,
+                                                             unsigned* __restrict__ out, int iters, int one) {
+    unsigned acc[2][8], a0[2], a1[2];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) a[r] = in[(threadIdx.x + r) & 255] & 0x3FFF3FFFu;
+    for (int r = 0; r < 2; ++r) {
+        a0[r] = in[(threadIdx.x + r) & 255] & 0x3FFF3FFFu;
+        a1[r] = in[256 + ((threadIdx.x + r) & 255)] & 0x3FFF3FFFu;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = in[256 + ((threadIdx.x + q) & 255)] & 0x3FFF3FFFu;
+        for (int c = 0; c < 8; ++c) acc[r][c] = in[512 + ((threadIdx.x + 8 * r + c) & 255)] & 0x3FFF3FFFu;
+    }
     for (int it = 0; it < iters; ++it) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) acc[q] = __viaddmin_u16x2(a[q & 3], acc[(q + 1) & 15], acc[q]);
+        for (int r = 0; r < 2; ++r) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const unsigned b0 = acc[r ^ 1][c];
+                const unsigned b1 = acc[r][(c + 1) & 7];
+                if (c < MIXW) {
+                    acc[r][c] = __viaddmin_u16x2(a1[r], b1, __viaddmin_u16x2(a0[r], b0, acc[r][c]));
+                } else {
+                    // lanes stay below 2^15, so the 32-bit sums carry nothing across lanes
+                    const unsigned s0 = (unsigned)add_on_fma((int)a0[r], (int)b0, one);
+                    const unsigned s1 = (unsigned)add_on_fma((int)a1[r], (int)b1, one);
+                    acc[r][c] = __vimin3_u16x2(acc[r][c], s0, s1);
+                }
+            }
+        }
     }
     unsigned s = 0;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) s ^= acc[q];
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) s ^= acc[r][c];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
@@ -94,42 +116,59 @@ int time_peak(int blocks, const int* in, int* out, cudaStream_t s, double* rate)
     return FW_OK;
 }
 
+template <int MIXW>
+int time_peak_packed(int blocks, const unsigned* in, unsigned* out, cudaStream_t s, double* rate) {
+    cudaEvent_t e0, e1;
+    FW_CUDA_TRY(cudaEventCreate(&e0));
+    FW_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(e0, s);
+        fw_peak_packed_kernel<MIXW><<<blocks, 256, 0, s>>>(in, out, kPeakIters, 1);
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_error(e, "fw_peak_packed_kernel");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;  // rep 0 warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // 16 accumulator words x 2 pivots x 2 lanes per iteration.
+    *rate = (double)blocks * 256.0 * kPeakIters * 64.0 / (best * 1e-3);
+    return FW_OK;
+}
+
 }  // namespace
 
-int measure_relax_peak_packed(double* packed, cudaStream_t s) {
+int measure_relax_peak_packed(double* dpx_only, double* mixed, cudaStream_t s) {
     int dev = 0, sms = 0;
     FW_CUDA_TRY(cudaGetDevice(&dev));
     FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int blocks = sms * 8;
     unsigned *in = nullptr, *out = nullptr;
-    FW_CUDA_TRY(cudaMallocAsync(&in, 512 * sizeof(unsigned), s));
+    FW_CUDA_TRY(cudaMallocAsync(&in, 768 * sizeof(unsigned), s));
     FW_CUDA_TRY(cudaMallocAsync(&out, (size_t)blocks * 256 * sizeof(unsigned), s));
-    FW_CUDA_TRY(cudaMemsetAsync(in, 0, 512 * sizeof(unsigned), s));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    float best = 1e30f;
-    int rc = FW_OK;
-    for (int rep = 0; rep < 5 && rc == FW_OK; ++rep) {
-        cudaEventRecord(e0, s);
-        fw_peak_packed_kernel<<<blocks, 256, 0, s>>>(in, out, kPeakIters);
-        cudaEventRecord(e1, s);
-        const cudaError_t e = cudaEventSynchronize(e1);
-        if (e != cudaSuccess) {
-            rc = cuda_error(e, "fw_peak_packed_kernel");
-            break;
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep > 0 && ms < best) best = ms;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    FW_CUDA_TRY(cudaMemsetAsync(in, 0, 768 * sizeof(unsigned), s));
+    // MIXW = 8: every word column as two packed DPX add-mins; the others: the
+    // packed remainder's mix (kP16MixA) and its neighbours.
+    double r8 = 0, r6 = 0, r5 = 0, r4 = 0, r3 = 0;
+    int rc = time_peak_packed<8>(blocks, in, out, s, &r8);
+    if (!rc) rc = time_peak_packed<6>(blocks, in, out, s, &r6);
+    if (!rc) rc = time_peak_packed<5>(blocks, in, out, s, &r5);
+    if (!rc) rc = time_peak_packed<4>(blocks, in, out, s, &r4);
+    if (!rc) rc = time_peak_packed<3>(blocks, in, out, s, &r3);
     cudaFreeAsync(in, s);
     cudaFreeAsync(out, s);
     if (rc) return rc;
-    // 16 accumulators x 2 lanes per iteration.
-    if (packed) *packed = (double)blocks * 256.0 * kPeakIters * 32.0 / (best * 1e-3);
+    if (dpx_only) *dpx_only = r8;
+    double best = r8;
+    for (double r : {r6, r5, r4, r3}) best = r > best ? r : best;
+    if (mixed) *mixed = best;
     return FW_OK;
 }
 

@@ -257,9 +257,11 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count);
  * the instruction mix the blocked kernels use (mixed). */
 int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream);
 
-/* The same for the packed 16-bit DPX add-min of FW_VARIANT_AUTO's fast path
- * (two relaxations per instruction). */
-int fw_measure_relax_peak_packed(double* packed, fw_stream_t stream);
+/* The same for the packed 16-bit form of FW_VARIANT_AUTO's fast path (two
+ * 15-bit lanes per word): every relaxation pair one packed DPX add-min
+ * (dpx_only), and the best rate of the packed kernels' instruction mix
+ * (mixed). */
+int fw_measure_relax_peak_packed(double* dpx_only, double* mixed, fw_stream_t stream);
 
 #ifdef __cplusplus
 }
