@@ -250,6 +250,16 @@ __device__ __forceinline__ void p_load_transposed_dup(uint32_t* dst, const uint1
 // 6 of 8 942, 5 of 8 922, 4 of 8 884, 3 of 8 930, 2 of 8 978 ms.
 constexpr int kP16MixA = 4;
 
+// Which word columns take the DPX form. With four of eight the even columns
+// do: the choice changes how the compiler schedules the two pipes (measured,
+// whole packed solve at n = 32768: even columns 875 ms, columns 0-3 884,
+// 2-5 894, {0,1,4,5} 895, {0,3,4,7} 919, odd 933, 4-7 947, rows 0-3 952,
+// checkerboard 989 ms).
+template <int MIXW>
+__device__ constexpr bool p_dpx_column(int w) {
+    return MIXW == 4 ? (w & 1) == 0 : w < MIXW;
+}
+
 template <int MIXW>
 __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t* As, const uint32_t* Bs, int tx,
                                              int ty, int one) {
@@ -276,7 +286,7 @@ __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t
         for (int r = 0; r < 8; ++r)
 #pragma unroll
             for (int w = 0; w < 8; ++w) {
-                if (w < MIXW) {
+                if (p_dpx_column<MIXW>(w)) {
                     c[r][w] = __viaddmin_u16x2(a1[r], b1[w], __viaddmin_u16x2(a0[r], b0[w], c[r][w]));
                 } else {
                     const uint32_t s0 = (uint32_t)add_on_fma((int)a0[r], (int)b0[w], one);
