@@ -254,7 +254,8 @@ constexpr int kP16MixA = 4;
 // do: the choice changes how the compiler schedules the two pipes (measured,
 // whole packed solve at n = 32768: even columns 875 ms, columns 0-3 884,
 // 2-5 894, {0,1,4,5} 895, {0,3,4,7} 919, odd 933, 4-7 947, rows 0-3 952,
-// checkerboard 989 ms).
+// checkerboard 989 ms; interleaved patterns of other counts: five columns
+// 899-927 ms, six 923-965, three 938 ms).
 template <int MIXW>
 __device__ constexpr bool p_dpx_column(int w) {
     return MIXW == 4 ? (w & 1) == 0 : w < MIXW;
