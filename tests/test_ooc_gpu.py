@@ -79,3 +79,19 @@ def test_beyond_reference_max_n(fw, cuda, oracle):
     out = h.numpy()
     for r in rows:
         assert np.array_equal(out[r], W_rows[r]), r
+
+
+@pytest.mark.parametrize("W,H", [(1024, 512), (4096, 0), (6016, 1024)])
+def test_wide_passes_match_in_core(fw, cuda, W, H):
+    """Pass widths from a sixth of n up to all of it (one pass), against the
+    in-core int32 sweep of the same matrix."""
+    torch = cuda
+    n = 6000
+    d = torch.empty((n, n), dtype=torch.int32, device="cuda")
+    fw.generate_graph_device(d, n, 0.4, 99, 1, 100)
+    h = torch.empty((n, n), dtype=torch.int32).pin_memory()
+    h.copy_(d)
+    fw.apsp_i32(d, n, 32, 8, fw.VARIANT_MULTI_LAYER, None)
+    fw.apsp_i32_host(h, n, W, H)
+    torch.cuda.synchronize()
+    assert torch.equal(d.cpu(), h)
