@@ -45,6 +45,7 @@
 #include <mutex>
 #include <random>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -285,20 +286,28 @@ int ensure_jump_tables(size_t chunks) {
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         const size_t workers = std::min<size_t>({(size_t)hw, (size_t)16, (todo + 3) / 4});
         const size_t per = (todo + workers - 1) / workers;
+        // A range reads only entries no other thread writes: the ones that
+        // existed before this call, else its own start power.
         auto fill = [&](size_t lo, size_t hi) {
-            Poly acc = t.r[lo - 1];
-            if (lo - 1 >= have) acc = g_power(t.field, t.g, lo - 1);
+            Poly acc = lo - 1 < have ? t.r[lo - 1] : g_power(t.field, t.g, lo - 1);
             for (size_t c = lo; c < hi; ++c) {
                 acc = t.field.mul(acc, t.g);
                 t.r[c] = acc;
             }
         };
         std::vector<std::thread> pool;
+        std::vector<std::pair<size_t, size_t>> here;  // ranges no thread could be started for
         for (size_t w = 1; w < workers; ++w) {
             const size_t lo = have + w * per, hi = std::min(chunks, have + (w + 1) * per);
-            if (lo < hi) pool.emplace_back(fill, lo, hi);
+            if (lo >= hi) continue;
+            try {
+                pool.emplace_back(fill, lo, hi);
+            } catch (const std::system_error&) {
+                here.emplace_back(lo, hi);
+            }
         }
         fill(have, std::min(chunks, have + per));
+        for (const auto& [lo, hi] : here) fill(lo, hi);
         for (auto& th : pool) th.join();
     }
     return FW_OK;
