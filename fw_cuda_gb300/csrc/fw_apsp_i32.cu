@@ -453,13 +453,15 @@ struct Blocked {
 template <bool VEC>
 int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahead, int* colT, int* rowP, int sets,
                        cudaStream_t s, const unsigned* skip) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_remainder_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-        attr_done = true;
-    }
+    static PerDeviceOnce attrs;
+    if (int rc = once_per_device(attrs, [] {
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_panel_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_remainder_kernel<VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+            return (int)FW_OK;
+        }))
+        return rc;
     Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip};
     b.ldp = (int64_t)b.T * kTile;
     {

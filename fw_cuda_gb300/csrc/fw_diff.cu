@@ -478,14 +478,15 @@ size_t f32_workspace_bytes(int64_t n, int64_t batch) {
 // both blocks). The chain for block t+1 starts once block t-1's bulk is done.
 template <typename V>
 int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, KernelClass kc) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_nh_panel_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFTSmemBytes));
-        attr_done = true;
-    }
+    static PerDeviceOnce attrs;
+    if (int rc = once_per_device(attrs, [] {
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_nh_panel_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFSmemBytes));
+            FW_CUDA_TRY(cudaFuncSetAttribute(fw_nh_remainder_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kFTSmemBytes));
+            return (int)FW_OK;
+        }))
+        return rc;
     AuxStream aux;
     if (int rc = aux_stream_get(s, &aux)) return rc;
     const int T = (int)((n + kTile - 1) / kTile);

@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "fw103.h"
@@ -28,6 +29,26 @@ int cuda_error(cudaError_t e, const char* what);
         cudaError_t _e = cudaGetLastError();                           \
         if (_e != cudaSuccess) return ::fw::cuda_error(_e, what);      \
     } while (0)
+
+// Runs `fn` (returning a status) once per device, from any thread: kernel
+// attributes such as the dynamic shared-memory limit belong to the current
+// device's context, so a process that drives several GPUs sets them on each.
+struct PerDeviceOnce {
+    std::mutex mu;
+    uint64_t done = 0;  // bit d: done on device d (devices >= 64 run it every time)
+};
+
+template <class Fn>
+int once_per_device(PerDeviceOnce& once, Fn&& fn) {
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+    std::lock_guard<std::mutex> lk(once.mu);
+    if (once.done & bit) return FW_OK;
+    const int rc = fn();
+    if (rc == FW_OK) once.done |= bit;
+    return rc;
+}
 
 // Kernel classes timed by fw_profile_begin/fw_profile_end.
 enum KernelClass {

@@ -273,14 +273,15 @@ size_t ooc_device_bytes(int64_t n, int64_t W, int64_t H) {
 }
 
 int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_ooc_update_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_ooc_update_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-        attr_done = true;
-    }
+    static PerDeviceOnce attrs;
+    if (int rc = once_per_device(attrs, [] {
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_ooc_update_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+            FW_CUDA_TRY(cudaFuncSetAttribute(fw_ooc_update_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSmemBytes));
+            return (int)FW_OK;
+        }))
+        return rc;
     int dev = 0, sms = 0;
     FW_CUDA_TRY(cudaGetDevice(&dev));
     FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

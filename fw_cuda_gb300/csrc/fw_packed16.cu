@@ -582,14 +582,17 @@ size_t p16_workspace_bytes(int64_t n) {
 // skip. The sweep looks one pivot block ahead (two panel buffers): see the
 // schedule below.
 int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_p16_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
-        FW_CUDA_TRY(
-            cudaFuncSetAttribute(fw_p16_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
-        FW_CUDA_TRY(cudaFuncSetAttribute(fw_p16_cross_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
-        attr_done = true;
-    }
+    static PerDeviceOnce attrs;
+    if (int rc = once_per_device(attrs, [] {
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_p16_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_p16_remainder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+            FW_CUDA_TRY(
+                cudaFuncSetAttribute(fw_p16_cross_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes));
+            return (int)FW_OK;
+        }))
+        return rc;
     AuxStream aux;
     if (int rc = aux_stream_get(s, &aux)) return rc;
     const int64_t ld = p16_ld(n);
