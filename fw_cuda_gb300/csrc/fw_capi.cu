@@ -3,6 +3,7 @@
 // host-side graph generator.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -33,7 +34,7 @@ std::map<std::pair<int, cudaStream_t>, const unsigned int*> g_auto_done;
 
 // ----------------------------------------------------------------- profiling
 struct ProfState {
-    bool on = false;
+    std::atomic<bool> on{false};
     std::vector<cudaEvent_t> pool;
     size_t next = 0;
     struct Rec {
@@ -106,6 +107,8 @@ void* workspace_get(cudaStream_t s, size_t bytes) {
         cudaFree(w.ptr);
         w.ptr = nullptr;
         w.bytes = 0;
+        // an FW_VARIANT_AUTO report of this stream pointed into it
+        g_auto_done.erase({dev, s});
     }
     void* p = nullptr;
     const cudaError_t e = cudaMalloc(&p, bytes);

@@ -67,7 +67,10 @@ int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_st
 /* After a FW_VARIANT_AUTO call on `stream`: synchronises the stream and sets
  * *used_packed to 1 if the exact packed 16-bit sweep produced the result, 0 if
  * the int32 sweep ran (input outside [0, 32767) u {INF}, or distances too
- * close to the 16-bit cap to prove the packed result exact). */
+ * close to the 16-bit cap to prove the packed result exact). The answer lives
+ * in the call's workspace: ask before freeing a caller workspace
+ * (fw_apsp_i32_ws); a library workspace that a later, larger call on the
+ * stream replaced makes this return FW_ERR_INVALID_ARGUMENT. */
 int fw_apsp_auto_report(fw_stream_t stream, int* used_packed);
 
 /* Bytes of device workspace fw_apsp_i32_ws needs for these arguments. */
