@@ -446,6 +446,12 @@ int fw_batch_plan_describe(const fw_batch_plan* p, char* buf, size_t cap, double
 
 int fw_apsp_batched_i32(fw_batch_plan* p, int32_t* d_packed, fw_stream_t stream) {
     if (!p || !d_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_batched_i32: NULL plan or buffer");
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != p->device)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_batched_i32: the plan was created on device " +
+                                                      std::to_string(p->device) + ", the current device is " +
+                                                      std::to_string(dev));
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (p->exec == nullptr || p->exec_packed != d_packed) {
         drop_graph(p);
@@ -477,6 +483,12 @@ int fw_apsp_batched_i32(fw_batch_plan* p, int32_t* d_packed, fw_stream_t stream)
 // resident CTAs per SM for the whole batch. Synchronises the stream.
 int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_t stream) {
     if (!p || !d_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_batch_plan_autotune: NULL argument");
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != p->device)
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_batch_plan_autotune: the plan was created on device " +
+                                                      std::to_string(p->device) + ", the current device is " +
+                                                      std::to_string(dev));
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     int32_t* scratch = nullptr;
     const size_t bytes = sizeof(int32_t) * (size_t)p->total_elems;

@@ -172,7 +172,9 @@ int fw_batch_plan_create(fw_batch_plan** plan, const int32_t* h_sizes, const int
 int fw_batch_plan_autotune(fw_batch_plan* plan, const int32_t* d_packed, fw_stream_t stream);
 
 /* Solves every graph of the batch in place: one CUDA-graph launch (captured
- * on the first call for this d_packed, replayed afterwards). */
+ * on the first call for this d_packed, replayed afterwards). A plan belongs to
+ * the device it was created on and holds one work counter and one workspace:
+ * its solves must not overlap (one stream, or ordered by events). */
 int fw_apsp_batched_i32(fw_batch_plan* plan, int32_t* d_packed, fw_stream_t stream);
 
 /* The chosen schedule as text, and the batch's total relaxations (sum n^3). */
