@@ -178,6 +178,25 @@ def _ptr(x) -> int:
     raise TypeError(f"cannot take a device address of {type(x)!r}")
 
 
+def _dev(x, count: int, dtypes: tuple[str, ...], what: str) -> int:
+    """Device address of `x` after checking what the C-ABI call will touch: a
+    contiguous CUDA tensor of one of `dtypes` (names such as "int32") with at
+    least `count` elements. An int is a raw address and is passed unchecked."""
+    if isinstance(x, int):
+        return x
+    p = _ptr(x)
+    name = str(x.dtype).replace("torch.", "")
+    if name not in dtypes:
+        raise TypeError(f"{what}: expected dtype {' or '.join(dtypes)}, got {name}")
+    if x.numel() < count:
+        raise ValueError(f"{what}: needs at least {count} elements, got {x.numel()}")
+    return p
+
+
+def _sq(n: int, batch: int = 1) -> int:
+    return max(int(n), 0) ** 2 * max(int(batch), 0)
+
+
 def _stream(stream) -> int | None:
     if stream is None:
         return None
@@ -188,7 +207,7 @@ def _stream(stream) -> int | None:
 
 def apsp_i32(d_D, n: int, tile: int = 0, kappa: int = 0, variant: int = VARIANT_MULTI_LAYER, stream=None) -> None:
     """In-place APSP on the device (enqueued on `stream`; no synchronisation)."""
-    _check(lib().fw_apsp_i32(_ptr(d_D), n, tile, kappa, variant, _stream(stream)))
+    _check(lib().fw_apsp_i32(_dev(d_D, _sq(n), ("int32",), "d_D"), n, tile, kappa, variant, _stream(stream)))
 
 
 def auto_used_packed(stream=None) -> bool:
@@ -204,8 +223,11 @@ def workspace_bytes_i32(n: int, tile: int = 0, kappa: int = 0, variant: int = VA
 
 def apsp_i32_ws(d_D, n: int, workspace, workspace_bytes: int, tile: int = 0, kappa: int = 0,
                 variant: int = VARIANT_MULTI_LAYER, stream=None) -> None:
-    _check(lib().fw_apsp_i32_ws(_ptr(d_D), n, tile, kappa, variant, _ptr(workspace), workspace_bytes,
-                                _stream(stream)))
+    if not isinstance(workspace, int) and workspace.numel() * workspace.element_size() < workspace_bytes:
+        raise ValueError(f"workspace: holds {workspace.numel() * workspace.element_size()} bytes, "
+                         f"workspace_bytes says {workspace_bytes}")
+    _check(lib().fw_apsp_i32_ws(_dev(d_D, _sq(n), ("int32",), "d_D"), n, tile, kappa, variant, _ptr(workspace),
+                                workspace_bytes, _stream(stream)))
 
 
 def generate_graph(n: int, density: float, seed: int, wmin: int = 0, wmax: int = MAX_EDGE_WEIGHT,
@@ -221,7 +243,8 @@ def generate_graph(n: int, density: float, seed: int, wmin: int = 0, wmax: int =
 def generate_graph_device(d_D, n: int, density: float, seed: int, wmin: int = 0, wmax: int = MAX_EDGE_WEIGHT,
                           stream=None) -> None:
     """generate_graph's matrix, value for value, generated on the device into d_D."""
-    _check(lib().fw_generate_graph_device_i32(_ptr(d_D), n, float(density), seed, wmin, wmax, _stream(stream)))
+    _check(lib().fw_generate_graph_device_i32(_dev(d_D, _sq(n), ("int32",), "d_D"), n, float(density), seed, wmin,
+                                              wmax, _stream(stream)))
 
 
 def mt19937_outputs(seed: int, skip: int, count: int) -> np.ndarray:
@@ -277,7 +300,8 @@ def measure_relax_peak_packed(stream=None) -> tuple[float, float]:
 # ------------------------------------------------------ paths, graph I/O, checks
 def apsp_paths_i32(d_D, d_nh, n: int, batch: int = 1, stream=None) -> None:
     """In-place int32 APSP that also writes next hops into d_nh (int32, same shape)."""
-    _check(lib().fw_apsp_paths_i32(_ptr(d_D), _ptr(d_nh), n, batch, _stream(stream)))
+    _check(lib().fw_apsp_paths_i32(_dev(d_D, _sq(n, batch), ("int32",), "d_D"),
+                                   _dev(d_nh, _sq(n, batch), ("int32",), "d_nh"), n, batch, _stream(stream)))
 
 
 def path(nh: np.ndarray, i: int, j: int) -> list[int]:
@@ -293,14 +317,18 @@ def path(nh: np.ndarray, i: int, j: int) -> list[int]:
 
 def dense_from_csr(d_rowptr, d_col, d_w, n: int, d_D, d_bad=None, stream=None) -> None:
     """Dense int32 matrix (INF / 0 diagonal / min of duplicates) from a device CSR graph."""
-    _check(lib().fw_dense_from_csr_i32(_ptr(d_rowptr), _ptr(d_col) if d_col is not None else None,
-                                       _ptr(d_w) if d_w is not None else None, n, _ptr(d_D),
-                                       _ptr(d_bad) if d_bad is not None else None, _stream(stream)))
+    _check(lib().fw_dense_from_csr_i32(_dev(d_rowptr, max(int(n), 0) + 1, ("int64",), "d_rowptr"),
+                                       _dev(d_col, 0, ("int32",), "d_col") if d_col is not None else None,
+                                       _dev(d_w, 0, ("int32",), "d_w") if d_w is not None else None, n,
+                                       _dev(d_D, _sq(n), ("int32",), "d_D"),
+                                       _dev(d_bad, 1, ("int32", "uint32"), "d_bad") if d_bad is not None else None,
+                                       _stream(stream)))
 
 
 def negative_cycle_flags(d_D, n: int, batch: int, d_flags, stream=None) -> None:
     """d_flags[b] = 1 if graph b has a negative diagonal entry (hasNegativeCycle)."""
-    _check(lib().fw_negative_cycle_i32(_ptr(d_D), n, batch, _ptr(d_flags), _stream(stream)))
+    _check(lib().fw_negative_cycle_i32(_dev(d_D, _sq(n, batch), ("int32",), "d_D"), n, batch,
+                                       _dev(d_flags, max(int(batch), 0), ("int32",), "d_flags"), _stream(stream)))
 
 
 def apsp_i32_host(h_D, n: int, pass_width: int = 0, stripe_rows: int = 0, stream=None) -> None:
@@ -308,12 +336,16 @@ def apsp_i32_host(h_D, n: int, pass_width: int = 0, stripe_rows: int = 0, stream
     numpy array or CPU tensor), streamed through the device in row stripes;
     returns when h_D holds the result."""
     if hasattr(h_D, "data_ptr"):
-        if h_D.is_cuda or not h_D.is_contiguous():
-            raise ValueError("expected a contiguous CPU tensor")
+        if h_D.is_cuda or not h_D.is_contiguous() or str(h_D.dtype) != "torch.int32":
+            raise ValueError("expected a contiguous int32 CPU tensor")
+        if h_D.numel() < _sq(n):
+            raise ValueError(f"h_D: needs at least {_sq(n)} elements, got {h_D.numel()}")
         addr = h_D.data_ptr()
     elif isinstance(h_D, np.ndarray):
         if h_D.dtype != np.int32 or not h_D.flags.c_contiguous or not h_D.flags.writeable:
             raise ValueError("expected a writeable C-contiguous int32 array")
+        if h_D.size < _sq(n):
+            raise ValueError(f"h_D: needs at least {_sq(n)} elements, got {h_D.size}")
         addr = h_D.ctypes.data
     else:
         raise TypeError(f"cannot take a host address of {type(h_D)!r}")
@@ -345,17 +377,21 @@ class BatchPlan:
             offsets = np.ascontiguousarray(offsets, dtype=np.int64)
             self.total_elems = int(np.max(offsets + self.sizes.astype(np.int64) ** 2))
         self.offsets = offsets
+        # elements the solves touch (the packing's total may add alignment padding)
+        self.touched_elems = int(np.max(self.offsets + self.sizes.astype(np.int64) ** 2)) if len(self.sizes) else 0
         h = ctypes.c_void_p()
         _check(lib().fw_batch_plan_create(ctypes.byref(h), self.sizes.ctypes.data, self.offsets.ctypes.data,
                                           len(self.sizes)))
         self._h = h
 
     def autotune(self, d_packed, stream=None) -> str:
-        _check(lib().fw_batch_plan_autotune(self._h, _ptr(d_packed), _stream(stream)))
+        _check(lib().fw_batch_plan_autotune(self._h, _dev(d_packed, self.touched_elems, ("int32",), "d_packed"),
+                                            _stream(stream)))
         return self.describe()
 
     def solve(self, d_packed, stream=None) -> None:
-        _check(lib().fw_apsp_batched_i32(self._h, _ptr(d_packed), _stream(stream)))
+        _check(lib().fw_apsp_batched_i32(self._h, _dev(d_packed, self.touched_elems, ("int32",), "d_packed"),
+                                         _stream(stream)))
 
     def describe(self) -> str:
         buf = ctypes.create_string_buffer(512)

@@ -145,3 +145,46 @@ def test_library_missing_fails_loudly(monkeypatch):
     else:
         raise AssertionError("expected FwLibraryMissing")
     assert ctypes is not None
+
+
+class _FakeCudaTensor:
+    """Stands in for a CUDA tensor: the Python view checks dtype and size before
+    the C call, so none of these reaches the library."""
+
+    is_cuda = True
+
+    def __init__(self, dtype: str, numel: int):
+        self.dtype, self._numel = dtype, numel
+
+    def is_contiguous(self):
+        return True
+
+    def data_ptr(self):
+        return 1 << 20
+
+    def numel(self):
+        return self._numel
+
+    def element_size(self):
+        return 4
+
+
+def test_tensor_arguments_are_checked_before_the_call(fw):
+    T = _FakeCudaTensor
+    n = 10
+    with pytest.raises(TypeError):
+        fw.apsp_i32(T("torch.float32", n * n), n)
+    with pytest.raises(ValueError):
+        fw.apsp_i32(T("torch.int32", n * n - 1), n)
+    with pytest.raises(ValueError):
+        fw.generate_graph_device(T("torch.int32", 50), n, 0.5, 1)
+    with pytest.raises(ValueError):
+        fw.apsp_paths_i32(T("torch.int32", 3 * n * n), T("torch.int32", 3 * n * n - 1), n, 3)
+    with pytest.raises(TypeError):
+        fw.negative_cycle_flags(T("torch.int32", 2 * n * n), n, 2, T("torch.int64", 2))
+    with pytest.raises(ValueError):
+        fw.apsp_i32_ws(T("torch.int32", n * n), n, T("torch.int32", 8), 64)
+    with pytest.raises(TypeError):
+        fw.dense_from_csr(T("torch.int32", n + 1), None, None, n, T("torch.int32", n * n))
+    with pytest.raises(ValueError):
+        fw.apsp_i32_host(np.zeros(n * n - 1, dtype=np.int32), n)
