@@ -54,6 +54,11 @@ def forward_with_next_hops(W: torch.Tensor, stream=None):
 def backward_from_next_hops(G: torch.Tensor, nh: torch.Tensor, stream=None, check_walks: bool = False):
     """dL/dW from dL/dD = G and the forward's next hops."""
     batch, n = _shape(nh)
+    if nh.dtype != torch.int32 or not nh.is_cuda or nh.shape[-1] != n:
+        raise ValueError("nh must be the forward's square int32 CUDA next-hop tensor")
+    if tuple(G.shape) != tuple(nh.shape) or G.device != nh.device:
+        raise ValueError(f"G must have nh's shape {tuple(nh.shape)} and device, got {tuple(G.shape)} on {G.device}")
+    nh = nh.contiguous()
     G = G.contiguous().to(torch.float32)
     dW = torch.empty(nh.shape, dtype=torch.float32, device=nh.device)
     bad = torch.zeros(1, dtype=torch.int32, device=nh.device) if check_walks else None
