@@ -4,24 +4,29 @@
 
 Workload (default): the reference's maximum size, n = 32768 (a 4 GiB int32
 matrix), density 0.5, integer weights uniform in [1, 100], missing edge = INF,
-diagonal 0, seed 7, solved with the multi-layer (kappa = 4) schedule. Inputs
-are synthetic (the reference's generator with the weight range as a
-parameter). Metric: relaxations per second, n^3 per solve / solve time.
+diagonal 0, seed 7, solved by the drop-in for the reference's
+multi_layer_tiling_gpu (kappa = 8) in int32 arithmetic. Inputs are synthetic
+(the reference's generator with the weight range as a parameter). Metric:
+relaxations per second, n^3 per solve / solve time.
 
 One step = restore the pristine input (device-to-device copy) + one full
 solve. `value` is timed on the device with CUDA events over exactly K steps
 (inputs resident in HBM, 4 GiB > L2 so nothing stays cached between steps);
 `e2e` is the same metric through the C ABI with host buffers: every step
 copies the input from pinned host memory, solves, and copies the distance
-matrix back. With --gpus N (torchrun) every rank solves its own copy of the
-workload (replicas; the path has no data-parallel exchange) and `value` is
-the sum over ranks, timed by the slowest rank.
+matrix back. `auto_path` is the same workload through FW_VARIANT_AUTO (the
+exact packed 16-bit fast path, taken only when provably identical), with its
+own roofline and e2e; `verified` compares its result with the int32 result
+bit for bit and checks sampled full rows of the int32 result against the
+oracle's Dijkstra. With --gpus N (torchrun) every rank solves its own copy of
+the workload (replicas; the path has no data-parallel exchange) and `value`
+is the sum over ranks, timed by the slowest rank.
 
 --impl reference times the reference's CPU implementation of the path
 (baseline_cpu, src/fw_baseline_cpu.cpp:3-16, as restated by the oracle) on
 all host cores over bounded samples of the same workload, and additionally
-the reference's own GPU kernels (multi_layer_tiling_gpu, kappa 4, built for
-sm_103a from its sources) on the full workload.
+the reference's own GPU kernels (multi_layer_tiling_gpu, the run's kappa,
+built for sm_103a from its sources) on the full workload.
 """
 from __future__ import annotations
 
@@ -58,11 +63,12 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--wmin", type=int, default=1)
     ap.add_argument("--wmax", type=int, default=100)
-    ap.add_argument("--algorithm", default="auto", choices=list(VARIANTS),
-                    help="auto = exact packed 16-bit sweep when provably identical, else multi_layer_tiling_gpu")
+    ap.add_argument("--algorithm", default="multi_layer_tiling_gpu", choices=list(VARIANTS),
+                    help="the headline; auto = exact packed 16-bit sweep when provably identical, else "
+                         "multi_layer_tiling_gpu")
     ap.add_argument("--kappa", type=int, default=8)
-    ap.add_argument("--no-int32", action="store_true",
-                    help="skip the extra timing of the int32 multi-layer sweep next to an auto run")
+    ap.add_argument("--no-auto", action="store_true",
+                    help="skip the sub-record of the exact packed fast path (FW_VARIANT_AUTO)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target length of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -169,6 +175,190 @@ def aggregate(world: int, steps: int, relax_per_step: float, elapsed_s: float) -
     return world * steps * relax_per_step / elapsed_s
 
 
+def solve_steps(F, torch, stream, work, pristine, n, kappa, variant, steps, warmup, world, local=None):
+    """`warmup` untimed then `steps` timed restore + solve steps of `variant`
+    on `stream` (CUDA events, per-kernel profile over the timed steps). With
+    `local` set, nvidia-smi clocks are sampled during the timed region."""
+    def step():
+        work.copy_(pristine, non_blocking=True)
+        F.apsp_i32(work, n, 32, kappa, variant, stream)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local if local is not None else 0)
+    if local is not None:
+        clocks.__enter__()
+    try:
+        F.profile_begin()
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        prof = F.profile_end()
+    finally:
+        if local is not None:
+            clocks.__exit__(None, None, None)
+    barrier(world)
+    F.check_faults(stream)
+    elapsed = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    return elapsed, prof, (clocks.summary() if local is not None else None)
+
+
+def end_to_end(F, torch, stream, work, h_in, n, kappa, variant, steps, world, local, relax, serial_steps):
+    """The metric through the C ABI with host buffers: every step copies its
+    input from pinned host memory and its result back. Pipelined over two
+    device buffers (as a user streaming matrices would run it): step k+1's
+    host-to-device copy and step k-1's device-to-host copy run on their own
+    streams while step k solves. The serial form (copy, solve, copy) is timed
+    too, over `serial_steps` steps. Returns the e2e record and the host copy
+    of the last result."""
+    h_out = torch.empty((n, n), dtype=torch.int32).pin_memory()
+    bufs = [work, torch.empty_like(work)]
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def serial_step():
+        work.copy_(h_in, non_blocking=True)
+        F.apsp_i32(work, n, 32, kappa, variant, stream)
+        h_out.copy_(work, non_blocking=True)
+
+    def pipelined(k_steps):
+        ev_in = [torch.cuda.Event() for _ in bufs]
+        ev_solved = [torch.cuda.Event() for _ in bufs]
+        ev_out = [torch.cuda.Event() for _ in bufs]
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+
+        def copy_in(k):  # step k's input into buffer k % 2, once its previous result is home
+            i = k % 2
+            if k >= 2:
+                s_in.wait_event(ev_out[i])
+            with torch.cuda.stream(s_in):
+                bufs[i].copy_(h_in, non_blocking=True)
+            ev_in[i].record(s_in)
+
+        a.record(s_in)
+        copy_in(0)
+        for k in range(k_steps):
+            i = k % 2
+            # Enqueue the next input before this solve: the solve's ~2000
+            # launches can block the host until the GPU has run most of them.
+            if k + 1 < k_steps:
+                copy_in(k + 1)
+            stream.wait_event(ev_in[i])
+            F.apsp_i32(bufs[i], n, 32, kappa, variant, stream)
+            ev_solved[i].record(stream)
+            s_out.wait_event(ev_solved[i])
+            with torch.cuda.stream(s_out):
+                h_out.copy_(bufs[i], non_blocking=True)
+            ev_out[i].record(s_out)
+        b.record(s_out)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    def copy_rate(fn):
+        fn()
+        torch.cuda.synchronize()
+        x = torch.cuda.Event(enable_timing=True)
+        y = torch.cuda.Event(enable_timing=True)
+        x.record(stream)
+        fn()
+        y.record(stream)
+        torch.cuda.synchronize()
+        return 4.0 * n * n / (x.elapsed_time(y) / 1e3) / 1e9
+
+    h2d_gbs = copy_rate(lambda: work.copy_(h_in, non_blocking=True))
+    d2h_gbs = copy_rate(lambda: h_out.copy_(work, non_blocking=True))
+
+    serial_step()
+    pipelined(2)
+    torch.cuda.synchronize()
+    barrier(world)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t2 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as e2e_clocks:
+        e2e_s = max_over_ranks(pipelined(steps), world)
+        t1.record(stream)
+        for _ in range(serial_steps):
+            serial_step()
+        t2.record(stream)
+        torch.cuda.synchronize()
+    F.check_faults(stream)
+    serial_s = max_over_ranks(t1.elapsed_time(t2) / 1e3, world)
+    rec = {"value": aggregate(world, steps, relax, e2e_s), "unit": UNIT,
+           "h2d_bytes_per_step": 4 * n * n, "d2h_bytes_per_step": 4 * n * n,
+           "ms_per_step": 1e3 * e2e_s / steps, "pipelined": True,
+           "serial_ms_per_step": 1e3 * serial_s / serial_steps, "serial_steps": serial_steps,
+           "serial_value": aggregate(world, serial_steps, relax, serial_s),
+           "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "clocks": e2e_clocks.summary()}
+    # the two buffers solved the same input
+    rec["buffers_agree"] = bool(torch.equal(bufs[0], bufs[1]))
+    del bufs[1]
+    return rec, h_out
+
+
+def int32_ceiling(F, stream, sm_mhz):
+    """The int32 relaxation ceiling of this GPU from register-only kernels:
+    the best measured relaxation form (the roofline's peak) and a model from
+    the measured instruction-class rates. A relaxation is either one DPX
+    add-min (ALU pipe) or one multiply-add (FMA pipe) plus half of a DPX
+    three-way min (ALU pipe); with a fraction x of the first kind the ALU
+    needs (1 + x) / 2 lane operations per relaxation, the FMA pipe 1 - x, and
+    both together (3 - x) / 2, bounded by the add-min rate, the multiply-add
+    rate and the measured rate of the two classes alternating. The model's
+    best x is the most any int32 instruction mix of these classes can give."""
+    dpx_only, mixed = F.measure_relax_peak(stream)
+    rates = F.measure_int32_rates(stream)
+    forms = {"form_b_relax": rates["form_b_relax"], "form_a_relax": rates["form_a_relax"],
+             "form_b_then_addmin_relax": rates["form_b_then_addmin_relax"], "mixed_probe": mixed,
+             "dpx_only_probe": dpx_only}
+    best_name = max(forms, key=forms.get)
+    r_alu, r_fma, r_both = rates["dpx_addmin"], rates["imad"], rates["dpx_addmin_imad_alternating"]
+    best_x, best_r = 0.0, 0.0
+    for i in range(1001):
+        x = i / 1000.0
+        r = min(r_alu / ((1 + x) / 2), r_fma / (1 - x) if x < 1 else float("inf"), r_both / ((3 - x) / 2))
+        if r > best_r:
+            best_x, best_r = x, r
+    out = {"peak": forms[best_name], "peak_form": best_name, "forms_relax_per_s": forms,
+           "class_lane_ops_per_s": {k: rates[k] for k in ("dpx_addmin", "imad", "dpx_min3", "add", "min",
+                                                          "dpx_addmin_imad_alternating")},
+           "model_peak": best_r, "model_addmin_fraction": best_x}
+    if sm_mhz:
+        sms = torch_sm_count()
+        per = 1.0 / (sm_mhz * 1e6 * sms)
+        out["per_clock_per_sm"] = {"sm_mhz": sm_mhz, "sms": sms,
+                                   "class_warp_instr": {k: v * per / 32 for k, v in out["class_lane_ops_per_s"].items()},
+                                   "peak_relax": out["peak"] * per, "model_peak_relax": best_r * per}
+    return out
+
+
+def torch_sm_count() -> int:
+    import torch
+
+    return int(torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count)
+
+
+def dijkstra_rows(W: np.ndarray, D_rows: dict, threads: int) -> dict:
+    """Full rows of a solved matrix against the oracle's dense Dijkstra from the
+    same sources (exact for non-negative weights), in parallel threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=max(1, min(threads, len(D_rows)))) as ex:
+        refs = dict(zip(D_rows, ex.map(lambda src: O.sssp_row(W, src), list(D_rows))))
+    ok = [int(src) for src in D_rows if np.array_equal(refs[src], D_rows[src])]
+    return {"rows": sorted(int(s) for s in D_rows), "rows_vs_dijkstra": f"{len(ok)}/{len(D_rows)}",
+            "all_rows_match": len(ok) == len(D_rows), "seconds": round(time.perf_counter() - t0, 2)}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -198,127 +388,13 @@ def run_ours(args) -> None:
     gen_dev_s = time.time() - t0
     gen_dev_same = bool(torch.equal(work, pristine))
 
-    def step():
-        work.copy_(pristine, non_blocking=True)
-        F.apsp_i32(work, n, 32, args.kappa, variant, stream)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-
-    peak_dpx, peak_mixed = F.measure_relax_peak(stream)
-    torch.cuda.synchronize()
-
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        F.profile_begin()
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        prof = F.profile_end()
-    barrier(world)
-    elapsed = e0.elapsed_time(e1) / 1e3
-    elapsed = max_over_ranks(elapsed, world)
+    # ---- the headline: the named algorithm, timed over exactly `steps` steps
+    elapsed, prof, clocks = solve_steps(F, torch, stream, work, pristine, n, args.kappa, variant, args.steps,
+                                        args.warmup, world, local)
     value = aggregate(world, args.steps, relax, elapsed)
+    head_out = work.clone()  # the timed solve's result, for the checks below
+    head_packed = F.auto_used_packed(stream) if variant == VARIANTS["auto"] else False
 
-    # End to end through the C ABI with host buffers: every step copies its
-    # input from pinned host memory and its result back. Pipelined over two
-    # device buffers (as a user streaming matrices would run it): step k+1's
-    # host-to-device copy and step k-1's device-to-host copy run on their own
-    # streams while step k solves. The serial form (copy, solve, copy) is
-    # timed too.
-    e2e = None
-    if not args.no_e2e:
-        h_out = torch.empty((n, n), dtype=torch.int32).pin_memory()
-        bufs = [work, torch.empty_like(work)]
-        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
-
-        def serial_step():
-            work.copy_(h_in, non_blocking=True)
-            F.apsp_i32(work, n, 32, args.kappa, variant, stream)
-            h_out.copy_(work, non_blocking=True)
-
-        def pipelined(steps):
-            ev_in = [torch.cuda.Event() for _ in bufs]
-            ev_solved = [torch.cuda.Event() for _ in bufs]
-            ev_out = [torch.cuda.Event() for _ in bufs]
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-
-            def copy_in(k):  # step k's input into buffer k % 2, once its previous result is home
-                i = k % 2
-                if k >= 2:
-                    s_in.wait_event(ev_out[i])
-                with torch.cuda.stream(s_in):
-                    bufs[i].copy_(h_in, non_blocking=True)
-                ev_in[i].record(s_in)
-
-            a.record(s_in)
-            copy_in(0)
-            for k in range(steps):
-                i = k % 2
-                # Enqueue the next input before this solve: the solve's ~2000
-                # launches can block the host until the GPU has run most of them.
-                if k + 1 < steps:
-                    copy_in(k + 1)
-                stream.wait_event(ev_in[i])
-                F.apsp_i32(bufs[i], n, 32, args.kappa, variant, stream)
-                ev_solved[i].record(stream)
-                s_out.wait_event(ev_solved[i])
-                with torch.cuda.stream(s_out):
-                    h_out.copy_(bufs[i], non_blocking=True)
-                ev_out[i].record(s_out)
-            b.record(s_out)
-            torch.cuda.synchronize()
-            return a.elapsed_time(b) / 1e3
-
-        def copy_rate(fn):
-            fn()
-            torch.cuda.synchronize()
-            x = torch.cuda.Event(enable_timing=True)
-            y = torch.cuda.Event(enable_timing=True)
-            x.record(stream)
-            fn()
-            y.record(stream)
-            torch.cuda.synchronize()
-            return 4.0 * n * n / (x.elapsed_time(y) / 1e3) / 1e9
-
-        h2d_gbs = copy_rate(lambda: work.copy_(h_in, non_blocking=True))
-        d2h_gbs = copy_rate(lambda: h_out.copy_(work, non_blocking=True))
-
-        serial_step()
-        pipelined(2)
-        torch.cuda.synchronize()
-        barrier(world)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t2 = torch.cuda.Event(enable_timing=True)
-        with ClockSampler(local) as e2e_clocks:
-            e2e_s = max_over_ranks(pipelined(args.steps), world)
-            t1.record(stream)
-            for _ in range(args.steps):
-                serial_step()
-            t2.record(stream)
-            torch.cuda.synchronize()
-        serial_s = max_over_ranks(t1.elapsed_time(t2) / 1e3, world)
-        e2e = {"value": aggregate(world, args.steps, relax, e2e_s), "unit": UNIT,
-               "h2d_bytes_per_step": 4 * n * n, "d2h_bytes_per_step": 4 * n * n,
-               "ms_per_step": 1e3 * e2e_s / args.steps, "pipelined": True,
-               "serial_ms_per_step": 1e3 * serial_s / args.steps,
-               "serial_value": aggregate(world, args.steps, relax, serial_s),
-               "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "clocks": e2e_clocks.summary()}
-        # The host copy of the last result equals the device-timed solve of
-        # the same input.
-        e2e["matches_device_result"] = bool(torch.equal(h_out, bufs[(args.steps - 1) % 2].cpu())) and \
-            bool(torch.equal(bufs[0], bufs[1]))
-        del bufs[1]
-
-    used_packed = F.auto_used_packed(stream) if variant == VARIANTS["auto"] else False
-    peak_packed_dpx, peak_packed = F.measure_relax_peak_packed(stream) if used_packed else (None, None)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -326,46 +402,24 @@ def run_ours(args) -> None:
     except OSError:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    if variant == VARIANTS["baseline_gpu"]:
-        st = prof.get("fw_pivot_step")
-        roofline = None
-        if st and st["launches"]:
-            secs = st["total_ms"] / 1e3
-            # algorithmic bytes of a pivot launch: the matrix read once (4 n^2);
-            # writes are the entries that change, which the kernel alone stores
-            gbs = 4.0 * n * n * st["launches"] / secs / 1e9
-            roofline = {"kernel": "fw_pivot_step_vec_kernel" if n % 4 == 0 else "fw_pivot_step_kernel",
-                        "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
-                        else "fallback", "avg_launch_ms": st["total_ms"] / st["launches"],
-                        "traffic": (268.54e6 + 3.45e6) * (n / 8192.0) ** 2, "traffic_unit": "bytes per launch",
-                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of pivot 4000 at "
-                                          "n = 8192, scaled by n^2"}
-    elif used_packed:
-        roofline = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, 512, peak_packed,
-                               "measured live: register-only packed 16-bit relaxation kernels "
-                               "(fw_measure_relax_peak_packed), best instruction mix", hbm_peak, "hbm_gbs" in peaks,
-                               traffic_at_16384=537.49e6 + 444.44e6)
-        if roofline:
-            roofline["dpx_only_peak"] = peak_packed_dpx
-            roofline["frac_of_dpx_only"] = roofline["achieved"] / peak_packed_dpx
-            roofline["int32_dpx_only_peak"] = peak_dpx
-    else:
-        pair = variant == VARIANTS["multi_layer_tiling_gpu"] and args.kappa > 4 and n >= 24576
-        # bulk launch: all tiles outside two pivot blocks (the two-block pass,
-        # or the look-ahead of the one-block pass)
-        roofline = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 256 if pair else 128, 4,
-                               256, peak_mixed,
-                               "measured live: register-only relaxation kernels (fw_measure_relax_peak), "
-                               "best instruction mix", hbm_peak, "hbm_gbs" in peaks,
-                               traffic_at_16384=(1.11e9 + 983.25e6) if pair else (1.07e9 + 979.55e6))
-        if roofline:
-            roofline["dpx_only_peak"] = peak_dpx
-            roofline["frac_of_dpx_only"] = roofline["achieved"] / peak_dpx
-    int32_path = None
-    if variant == VARIANTS["auto"] and not args.no_int32:
-        int32_path = time_variant(F, torch, stream, work, pristine, n, args.kappa, VARIANTS["multi_layer_tiling_gpu"],
-                                  args.steps, world, relax)
+    hbm_measured = "hbm_gbs" in peaks
+    ceiling = int32_ceiling(F, stream, clocks.get("sm_mhz") if clocks else None)
+    torch.cuda.synchronize()
+    roofline = head_roofline(F, stream, prof, n, args, variant, head_packed, ceiling, hbm_peak, hbm_measured)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e, h_out = end_to_end(F, torch, stream, work, h_in, n, args.kappa, variant, args.steps, world, local, relax,
+                                max(1, min(args.steps, 5)))
+        # the host copy of the last result equals the device-timed solve of the same input
+        e2e["matches_device_result"] = bool(torch.equal(h_out, head_out.cpu())) and e2e.pop("buffers_agree")
+        del h_out
+
+    # ---- the exact packed fast path (FW_VARIANT_AUTO) as a labelled sub-record
+    auto = None
+    if variant != VARIANTS["auto"] and not args.no_auto:
+        auto = run_auto(args, F, torch, stream, work, pristine, h_in, n, world, local, relax, head_out, hbm_peak,
+                        hbm_measured)
 
     batched = None
     if not args.no_batched:
@@ -377,20 +431,36 @@ def run_ours(args) -> None:
 
     ooc = None
     if not args.no_ooc:
-        ooc = run_out_of_core(args, F, torch, h_in, work, n, world, relax)
+        ooc = run_out_of_core(args, F, torch, h_in, head_out, n, world, relax)
 
+    verified = {"fault_status": "fw_check_faults clean after every timed region"}
+    if auto is not None:
+        verified["auto_equals_int32"] = auto.pop("equals_headline")
+    if e2e is not None:
+        verified["e2e_equals_device_result"] = e2e["matches_device_result"]
+    if ooc is not None:
+        verified["out_of_core_equals_in_core"] = ooc["matches_in_core"]
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        # The CPU-baseline leg: the oracle's sweep timed on a sample, and the
+        # oracle's Dijkstra rows as the checker of the timed solve's result.
         cpu = cpu_sample(h_in.numpy(), threads=1, seconds=args.cpu_seconds)
+        rng = np.random.default_rng(2024)
+        srcs = sorted({0, n - 1, *[int(x) for x in rng.choice(n, size=min(n, 6), replace=False)]})
+        rows = {s: head_out[s].cpu().numpy() for s in srcs}
+        verified.update(dijkstra_rows(h_in.numpy(), rows, os.cpu_count() or 1))
 
     launches = sum(v["launches"] for v in prof.values())
     if rank == 0:
+        int32_arith = variant != VARIANTS["auto"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32" if int32_arith or not head_packed else "int32 result via exact packed u16x2 arithmetic",
+            "data": "synthetic",
             "config": {"workload": f"APSP n={n} density={args.density} weights U[{args.wmin},{args.wmax}] "
-                                   f"seed={args.seed} ({args.algorithm}, kappa={args.kappa})",
+                                   f"seed={args.seed}",
                        "n": n, "density": args.density, "seed": args.seed, "algorithm": args.algorithm,
                        "kappa": args.kappa, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (4 GiB matrix), restored from a pristine copy every step",
@@ -398,16 +468,84 @@ def run_ours(args) -> None:
                        "device_generator_matches": gen_dev_same},
             "gpu_launches": launches,
             "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()},
-            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks.summary(),
+            "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "verified": verified, "auto_path": auto,
             "batched": batched, "differentiable": diff, "out_of_core": ooc,
-            "path": ("packed16" if used_packed else "int32") if variant == VARIANTS["auto"] else "int32",
-            "int32_path": int32_path,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def head_roofline(F, stream, prof, n, args, variant, packed, ceiling, hbm_peak, hbm_measured):
+    """Roofline of the headline's dominant kernel."""
+    if variant == VARIANTS["baseline_gpu"]:
+        st = prof.get("fw_pivot_step")
+        if not st or not st["launches"]:
+            return None
+        secs = st["total_ms"] / 1e3
+        # algorithmic bytes of a pivot launch: the matrix read once (4 n^2);
+        # writes are the entries that change, which the kernel alone stores
+        gbs = 4.0 * n * n * st["launches"] / secs / 1e9
+        return {"kernel": "fw_pivot_step_vec_kernel" if n % 4 == 0 else "fw_pivot_step_kernel",
+                "bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if hbm_measured else "fallback",
+                "avg_launch_ms": st["total_ms"] / st["launches"],
+                "traffic": (268.54e6 + 3.45e6) * (n / 8192.0) ** 2, "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of pivot 4000 at "
+                                  "n = 8192, scaled by n^2"}
+    if packed:
+        return packed_roofline(F, stream, prof, n, hbm_peak, hbm_measured)
+    pair = variant == VARIANTS["multi_layer_tiling_gpu"] and args.kappa > 4 and n >= 24576
+    # bulk launch: all tiles outside two pivot blocks (the two-block pass, or
+    # the look-ahead of the one-block pass)
+    r = roofline_of(prof.get("fw_remainder"), "fw_remainder_kernel", n, 256 if pair else 128, 4, 256,
+                    ceiling["peak"], "measured live: best register-only int32 relaxation form "
+                    f"({ceiling['peak_form']}, fw_measure_relax_peak / fw_measure_int32_rates)", hbm_peak,
+                    hbm_measured, traffic_at_16384=(1.11e9 + 983.25e6) if pair else (1.07e9 + 979.55e6))
+    if r:
+        r["int32_ceiling"] = ceiling
+        r["frac_of_model_peak"] = r["achieved"] / ceiling["model_peak"]
+    return r
+
+
+def packed_roofline(F, stream, prof, n, hbm_peak, hbm_measured):
+    peak_packed_dpx, peak_packed = F.measure_relax_peak_packed(stream)
+    r = roofline_of(prof.get("fw_p16_remainder"), "fw_p16_remainder_kernel", n, 256, 2, 512, peak_packed,
+                    "measured live: register-only packed 16-bit relaxation kernels "
+                    "(fw_measure_relax_peak_packed), best instruction mix", hbm_peak, hbm_measured,
+                    traffic_at_16384=537.49e6 + 444.44e6)
+    if r:
+        r["dpx_only_peak"] = peak_packed_dpx
+        r["frac_of_dpx_only"] = r["achieved"] / peak_packed_dpx
+    return r
+
+
+def run_auto(args, F, torch, stream, work, pristine, h_in, n, world, local, relax, head_out, hbm_peak, hbm_measured):
+    """FW_VARIANT_AUTO on the same workload: the exact packed 16-bit sweep
+    (two 15-bit lanes per DPX instruction) when the encode/decode proof
+    holds, else the int32 sweep. Its result is compared bit for bit with the
+    headline's int32 result."""
+    steps = max(1, min(args.steps, 10))
+    elapsed, prof, clocks = solve_steps(F, torch, stream, work, pristine, n, args.kappa, VARIANTS["auto"], steps,
+                                        1, world, local)
+    used = F.auto_used_packed(stream)
+    same = bool(torch.equal(work, head_out))
+    out = {"algorithm": "auto (FW_VARIANT_AUTO)", "kappa": args.kappa,
+           "dtype": "int32 result via exact packed u16x2 arithmetic" if used else "int32",
+           "used_packed": used, "value": aggregate(world, steps, relax, elapsed), "unit": UNIT, "steps": steps,
+           "ms_per_step": 1e3 * elapsed / steps, "clocks": clocks, "equals_headline": same,
+           "roofline": packed_roofline(F, stream, prof, n, hbm_peak, hbm_measured) if used else None,
+           "kernels": {k: {"launches": v["launches"], "total_ms": round(v["total_ms"], 3)} for k, v in prof.items()}}
+    if not args.no_e2e:
+        e2e, h_out = end_to_end(F, torch, stream, work, h_in, n, args.kappa, VARIANTS["auto"], steps, world, local,
+                                relax, 1)
+        e2e["matches_device_result"] = bool(torch.equal(h_out, head_out.cpu())) and e2e.pop("buffers_agree")
+        out["e2e"] = e2e
+        del h_out
+    return out
 
 
 def roofline_of(stats, kernel, n, pivots, bytes_per_value, gap, peak, peak_source, hbm_peak, hbm_measured,
@@ -441,30 +579,6 @@ def roofline_of(stats, kernel, n, pivots, bytes_per_value, gap, peak, peak_sourc
         out["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk launch at "
                                  "n = 16384, scaled by (n - %d)^2" % gap)
     return out
-
-
-def time_variant(F, torch, stream, work, pristine, n, kappa, variant, steps, world, relax) -> dict:
-    """The same restore + solve steps with another variant (one warm-up step)."""
-    def step():
-        work.copy_(pristine, non_blocking=True)
-        F.apsp_i32(work, n, 32, kappa, variant, stream)
-
-    step()
-    torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    F.profile_begin()
-    a.record(stream)
-    for _ in range(steps):
-        step()
-    b.record(stream)
-    torch.cuda.synchronize()
-    prof = F.profile_end()
-    el = max_over_ranks(a.elapsed_time(b) / 1e3, world)
-    rem = prof.get("fw_remainder", {"launches": 0, "total_ms": 1.0, "relaxations": 0.0})
-    return {"algorithm": "multi_layer_tiling_gpu", "kappa": kappa, "value": aggregate(world, steps, relax, el),
-            "unit": UNIT, "ms_per_step": 1e3 * el / steps,
-            "remainder_relax_per_s": rem["relaxations"] / (rem["total_ms"] / 1e3)}
 
 
 def run_batched(args, F, torch, stream, world) -> dict:
@@ -604,7 +718,6 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import fw_cuda_gb300 as F
     from oracle import oracle as O
 
     n = args.n
@@ -649,14 +762,16 @@ def run_reference(args) -> None:
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_gpu": ref_gpu,
     }
-    del F
     print(json.dumps(line), flush=True)
 
 
-def reference_gpu(args, W: np.ndarray):
-    """The reference's multi_layer_tiling_gpu (kappa 4) kernels, built for
-    sm_103a from its sources, timed on the full workload (one warm-up solve at
-    n=1024 first)."""
+def reference_gpu(args, W: np.ndarray, timed: int = 3):
+    """The reference's multi_layer_tiling_gpu kernels (the run's kappa), built
+    for sm_103a from its sources and launched by its own launch loop on the
+    legacy default stream, on the full workload: one untimed full-size solve,
+    then `timed` solves of a fresh copy of the input, each bracketed by CUDA
+    events on that stream (the reference's Timer::measureGPU also times one
+    solve with events after a warm-up, src/timer.cu:35-64)."""
     try:
         import torch
 
@@ -665,18 +780,28 @@ def reference_gpu(args, W: np.ndarray):
         if not torch.cuda.is_available() or not O.refgpu_available():
             return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
         n = W.shape[0]
-        warm = torch.from_numpy(np.ascontiguousarray(W[:1024, :1024])).cuda()
-        O.refgpu_run("multi_layer_tiling_gpu", warm.data_ptr(), 1024, args.kappa)
-        d = torch.from_numpy(W).cuda()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        O.refgpu_run("multi_layer_tiling_gpu", d.data_ptr(), n, args.kappa)
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        return {"algorithm": "multi_layer_tiling_gpu", "kappa": args.kappa, "value": float(n) ** 3 / el,
-                "unit": UNIT, "seconds_per_solve": el,
-                "how": "reference kernels (src/fw_multi_layer_tiling_gpu.cu) compiled for sm_103a, replayed with "
-                       "the reference launch loop, one solve timed on the host around a device synchronisation"}
+        legacy = torch.cuda.default_stream()
+        pristine = torch.from_numpy(W).cuda()
+        d = torch.empty_like(pristine)
+        secs = []
+        for i in range(1 + timed):
+            d.copy_(pristine)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(legacy)
+            O.refgpu_run("multi_layer_tiling_gpu", d.data_ptr(), n, args.kappa)  # synchronises the context
+            b.record(legacy)
+            b.synchronize()
+            if i > 0:
+                secs.append(a.elapsed_time(b) / 1e3)
+        mean = sum(secs) / len(secs)
+        return {"algorithm": "multi_layer_tiling_gpu", "kappa": args.kappa, "value": float(n) ** 3 / mean,
+                "unit": UNIT, "seconds_per_solve": mean, "seconds_min": min(secs), "seconds_max": max(secs),
+                "solves_timed": len(secs),
+                "how": "reference kernels (src/fw_multi_layer_tiling_gpu.cu) compiled for sm_103a, launched by the "
+                       "reference launch loop on the legacy default stream; one full-size warm-up solve, then "
+                       "CUDA events around each timed solve of a fresh copy of the input"}
     except Exception as e:  # report, never fail the CPU line
         return {"unavailable": f"{type(e).__name__}: {e}"}
 

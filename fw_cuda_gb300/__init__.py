@@ -65,7 +65,16 @@ EXPORTED_SYMBOLS = (
     "fw_apsp_batched_i32",
     "fw_batch_plan_describe",
     "fw_batch_plan_destroy",
+    "fw_apsp_i32_noalloc",
+    "fw_check_faults",
+    "fw_debug_inject",
+    "fw_debug_bounded_wait",
+    "fw_measure_int32_rates",
 )
+
+# Host-side fault injection kinds of fw_debug_inject (tests only).
+INJECT_CALL_FAULT = 1
+INJECT_PACKED_FAULT = 2
 
 
 class FwError(RuntimeError):
@@ -156,6 +165,16 @@ def lib():
     L.fw_batch_plan_describe.restype = c_int
     L.fw_batch_plan_destroy.argtypes = [vp]
     L.fw_batch_plan_destroy.restype = None
+    L.fw_apsp_i32_noalloc.argtypes = [vp, i64, c_int, c_int, c_int, vp]
+    L.fw_apsp_i32_noalloc.restype = c_int
+    L.fw_check_faults.argtypes = [vp, ctypes.POINTER(ctypes.c_uint)]
+    L.fw_check_faults.restype = c_int
+    L.fw_debug_inject.argtypes = [c_int]
+    L.fw_debug_inject.restype = c_int
+    L.fw_debug_bounded_wait.argtypes = [c_int, vp]
+    L.fw_debug_bounded_wait.restype = c_int
+    L.fw_measure_int32_rates.argtypes = [ctypes.POINTER(ctypes.c_double), c_int, vp]
+    L.fw_measure_int32_rates.restype = c_int
     _lib = L
     return L
 
@@ -255,10 +274,30 @@ def mt19937_outputs(seed: int, skip: int, count: int) -> np.ndarray:
 
 
 def copy_faults() -> int:
-    """Remainder-kernel tile copies that missed their bounded wait (0 when healthy)."""
+    """Tile copies that missed their bounded wait since the library was loaded (0 when healthy)."""
     c = ctypes.c_uint(0)
     _check(lib().fw_copy_faults(ctypes.byref(c)))
     return int(c.value)
+
+
+def check_faults(stream=None) -> None:
+    """Synchronises `stream` and raises FwError(FW_ERR_TIMEOUT) when the last
+    sweep call on it had a tile copy that missed its bounded wait (its result
+    is then not valid)."""
+    c = ctypes.c_uint(0)
+    _check(lib().fw_check_faults(_stream(stream), ctypes.byref(c)))
+
+
+def debug_inject(kinds: int) -> None:
+    """Test hook: host-side fault injection for the next call on this thread
+    (INJECT_CALL_FAULT, INJECT_PACKED_FAULT; 0 clears)."""
+    _check(lib().fw_debug_inject(kinds))
+
+
+def debug_bounded_wait(spins: int, stream=None) -> int:
+    """Test hook: a bounded wait on a copy that is never issued; returns the
+    status (FW_ERR_TIMEOUT when the wait gave up, as it should)."""
+    return int(lib().fw_debug_bounded_wait(spins, _stream(stream)))
 
 
 def version() -> str:
@@ -288,6 +327,18 @@ def measure_relax_peak(stream=None) -> tuple[float, float]:
     a, b = ctypes.c_double(0), ctypes.c_double(0)
     _check(lib().fw_measure_relax_peak(ctypes.byref(a), ctypes.byref(b), _stream(stream)))
     return a.value, b.value
+
+
+INT32_RATE_NAMES = ("dpx_addmin", "imad", "dpx_min3", "add", "min", "dpx_addmin_imad_alternating",
+                    "form_b_relax", "form_a_relax", "form_b_then_addmin_relax")
+
+
+def measure_int32_rates(stream=None) -> dict:
+    """Register-only int32 rates (fw_measure_int32_rates): lane operations/s of
+    each instruction class and relaxations/s of each relaxation form."""
+    r = (ctypes.c_double * len(INT32_RATE_NAMES))()
+    _check(lib().fw_measure_int32_rates(r, len(INT32_RATE_NAMES), _stream(stream)))
+    return dict(zip(INT32_RATE_NAMES, list(r)))
 
 
 def measure_relax_peak_packed(stream=None) -> tuple[float, float]:
@@ -418,11 +469,17 @@ class BatchPlan:
 
 # ----------------------------------------------------- reference-style registry
 def _synchronising(variant: int):
+    """The reference's launcher contract in Python: enqueue on the legacy
+    default stream, return after the device is synchronised, and fail (here:
+    raise FwError) on any error, a missed tile copy included. The C++ shims
+    with the same names (libfw103.so) print and exit instead, as the
+    reference does."""
     def algo(d_D, n: int, tileSize: int = 0, kappa: int = 0) -> None:
         import torch
 
         apsp_i32(d_D, n, tileSize, kappa, variant, None)
         torch.cuda.synchronize()
+        check_faults(None)
 
     return algo
 

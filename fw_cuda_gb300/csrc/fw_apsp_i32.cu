@@ -30,6 +30,7 @@
 // taken by the previous launch, so no launch reads what it writes.
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <utility>
 
 #include "fw_common.cuh"
@@ -42,6 +43,9 @@ namespace fw {
 // Tile copies that did not arrive within the bounded wait (a correct build
 // never counts one); read by fw_copy_faults.
 __device__ unsigned int g_copy_faults = 0;
+// Outcome of fw_debug_bounded_wait's kernel: bit 0 the wait gave up, bit 1
+// the barrier completed once its transfer count was settled.
+__device__ unsigned int g_wait_probe_result = 0;
 
 namespace {
 
@@ -153,11 +157,15 @@ __global__ void __launch_bounds__(kThreads, 2)
 // With cross >= 0 the tiles are instead block `cross`'s update of block
 // u = cross + 1's row and column: tiles [0, nrows - 1) are (u, J), J != cross,
 // the next nrows - 2 are (I, u), I != cross, u (nrows = T, ncols = 2T - 3).
+// A copy that misses its bounded wait is counted in `faults` (the call's
+// status word) and in g_copy_faults; the CTA then waits for the copies it
+// already issued, leaves that tile and every later tile of its share as they
+// were, and returns.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_remainder_kernel(int* __restrict__ D, int64_t n, TileSet rows, int nrows, TileSet cols, int ncols, int slab0,
                         int nslab, const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                        int one, const unsigned* __restrict__ skip, int cross) {
+                        int one, const unsigned* __restrict__ skip, int cross, unsigned* __restrict__ faults) {
     if (skip && *skip) return;
     extern __shared__ __align__(128) int smem[];
     __shared__ __align__(8) uint64_t bars[kStages];
@@ -167,12 +175,14 @@ __global__ void __launch_bounds__(kThreads, 2)
         // TMA destinations must be 128-byte aligned; the stage sizes keep every
         // stage and operand aligned when the base is.
         s_ok = (smem_u32(smem) & 127u) == 0;
-        if (!s_ok) atomicAdd(&g_copy_faults, 1u);
         for (int i = 0; i < kStages; ++i) mbar_init(&bars[i], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    const bool ok = s_ok != 0;
+    if (!s_ok) {  // no copy can be issued: the CTA's tiles keep their values
+        if (tid == 0) count_copy_fault(&g_copy_faults, faults);
+        return;
+    }
     // Operand slabs, k-major 32 x 128 ints each, by TMA: slab j of the CTA's
     // running count g + j goes to stage (g + j) % kStages, whose barrier
     // completes for the ((g + j) / kStages)-th time.
@@ -192,7 +202,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
         const int r0 = I * kTile, c0 = J * kTile;
         auto issue = [&](int j) {
-            if (tid == 0 && ok) {
+            if (tid == 0) {
                 const int stg = (g + j) % kStages;
                 int* dst = smem + stg * kStageInts;
                 mbar_expect_tx(&bars[stg], (uint32_t)kStageInts * 4);
@@ -205,23 +215,43 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
         for (int j = 0; j < kStages - 1; ++j)
             if (j < nslab) issue(j);
-        bool arrived = true;
         for (int kb = 0; kb < nslab; ++kb) {
             const int stg = (g + kb) % kStages;
-            if (ok && !mbar_wait(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
-                if (arrived) atomicAdd(&g_copy_faults, 1u);
-                arrived = false;
+            // every thread is past slab kb - 1 (its stage can be refilled), and
+            // all agree whether slab kb arrived
+            if (!ring_wait_all(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
+                if (tid == 0) count_copy_fault(&g_copy_faults, faults);
+                ring_drain(bars, kStages, g + kb, g + min(kb + kStages - 2, nslab - 1));
+                return;
             }
-            __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
             if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
-            if (ok && arrived) {
-                const int* st = smem + stg * kStageInts;
-                relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
-            }
+            const int* st = smem + stg * kStageInts;
+            relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
         }
         g += nslab;
         store_acc<VEC>(acc, D, n, r0, c0, tx, ty);
         __syncthreads();  // the next tile's prologue refills the ring
+    }
+}
+
+// Test kernel of fw_debug_bounded_wait: the remainder kernels' bounded wait
+// on a barrier whose 16-byte transfer is never issued. Afterwards thread 0
+// completes the transfer count itself, so the barrier ends balanced.
+__global__ void fw_wait_probe_kernel(int spins, unsigned* __restrict__ result) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);
+    __syncthreads();
+    const bool got = mbar_wait(&bar, 0u, spins);
+    const bool gave_up = __syncthreads_or(got ? 0 : 1) != 0;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(16u) : "memory");
+        const bool after = mbar_wait(&bar, 0u, 1024);
+        *result = (gave_up ? 1u : 0u) | (after ? 2u : 0u);
     }
 }
 
@@ -314,6 +344,7 @@ struct Blocked {
     int* rowP;
     cudaStream_t s;
     const unsigned* skip;
+    unsigned* faults;             // the call's status word (missed copies), may be null
     int64_t resident_ctas = 304;  // CTAs of the persistent remainder: 2 per SM
     AuxStream aux{};
     CUtensorMap mapA{}, mapB{};   // TMA maps over colT and rowP (all panel rows of the workspace)
@@ -354,7 +385,7 @@ struct Blocked {
         const unsigned grid = (unsigned)((skip && ntiles > resident_ctas) ? resident_ctas : ntiles);
         prof_begin(KC_REMAINDER, q);
         fw_remainder_kernel<VEC><<<grid, kThreads, kSmemBytes, q>>>(D, n, rows, nrows, cols, ncols, slab0, nslab, mapA,
-                                                                    mapB, 1, skip, cross);
+                                                                    mapB, 1, skip, cross, faults);
         FW_LAUNCH_CHECK("fw_remainder_kernel");
         const double relax = cross >= 0
                                  ? ((double)kv(cross + 1) * (double)(n - kv(cross)) +
@@ -452,7 +483,7 @@ struct Blocked {
 
 template <bool VEC>
 int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahead, int* colT, int* rowP, int sets,
-                       cudaStream_t s, const unsigned* skip) {
+                       cudaStream_t s, const unsigned* skip, unsigned* faults) {
     static PerDeviceOnce attrs;
     if (int rc = once_per_device(attrs, [] {
             FW_CUDA_TRY(
@@ -462,7 +493,7 @@ int blocked_solve_impl(int32_t* D, int64_t n, int blocks_per_pass, bool lookahea
             return (int)FW_OK;
         }))
         return rc;
-    Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip};
+    Blocked<VEC> b{D, n, 0, (int)((n + kTile - 1) / kTile), colT, rowP, s, skip, faults};
     b.ldp = (int64_t)b.T * kTile;
     {
         int dev = 0, sms = 0;
@@ -503,7 +534,7 @@ size_t blocked_workspace_bytes(int64_t n, int blocks) {
 }
 
 int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, size_t ws_bytes, cudaStream_t s,
-                  const unsigned int* skip) {
+                  const unsigned int* skip, unsigned int* faults) {
     const int64_t T = (n + kTile - 1) / kTile;
     // Two panel buffers are needed by the two-block pass and by the look-ahead.
     const bool two = ws_bytes >= blocked_workspace_bytes(n, 2);
@@ -511,8 +542,8 @@ int blocked_solve(int32_t* D, int64_t n, int blocks, void* ws, size_t ws_bytes, 
     int* colT = static_cast<int*>(ws);
     int* rowP = colT + (size_t)sets * kTile * (size_t)(T * kTile);
     const bool vec = (n % 4) == 0;
-    return vec ? blocked_solve_impl<true>(D, n, blocks, two, colT, rowP, sets, s, skip)
-               : blocked_solve_impl<false>(D, n, blocks, two, colT, rowP, sets, s, skip);
+    return vec ? blocked_solve_impl<true>(D, n, blocks, two, colT, rowP, sets, s, skip, faults)
+               : blocked_solve_impl<false>(D, n, blocks, two, colT, rowP, sets, s, skip, faults);
 }
 
 size_t pivot_workspace_bytes(int64_t n) { return (size_t)4 * (size_t)((n + 3) & ~int64_t(3)) * sizeof(int); }
@@ -544,6 +575,27 @@ int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
 }
 
 }  // namespace fw
+
+extern "C" int fw_debug_bounded_wait(int spins, fw_stream_t stream) {
+    if (spins < 1 || spins > (1 << 20))
+        return fw::set_error(FW_ERR_INVALID_ARGUMENT, "fw_debug_bounded_wait: spins must be in [1, 1048576]");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned int* result = nullptr;
+    FW_CUDA_TRY(cudaGetSymbolAddress(reinterpret_cast<void**>(&result), fw::g_wait_probe_result));
+    FW_CUDA_TRY(cudaMemsetAsync(result, 0, sizeof(unsigned int), s));
+    fw::fw_wait_probe_kernel<<<1, 32, 0, s>>>(spins, result);
+    FW_LAUNCH_CHECK("fw_wait_probe_kernel");
+    FW_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned int v = 0;
+    FW_CUDA_TRY(cudaMemcpy(&v, result, sizeof(v), cudaMemcpyDeviceToHost));
+    if (!(v & 2u))
+        return fw::set_error(FW_ERR_INTERNAL, "fw_debug_bounded_wait: the barrier did not complete after its "
+                                              "transfer count was settled");
+    if (v & 1u)
+        return fw::set_error(FW_ERR_TIMEOUT, "fw_debug_bounded_wait: the bounded wait gave up after " +
+                                                 std::to_string(spins) + " tries (no copy was issued)");
+    return FW_OK;
+}
 
 extern "C" int fw_copy_faults(unsigned int* count) {
     if (count == nullptr) return fw::set_error(FW_ERR_INVALID_ARGUMENT, "fw_copy_faults: count is NULL");

@@ -31,6 +31,12 @@ std::map<std::pair<int, cudaStream_t>, WsEntry> g_ws;
 // Device address of the packed path's `done` word of the last FW_VARIANT_AUTO
 // call per (device, stream), for fw_apsp_auto_report.
 std::map<std::pair<int, cudaStream_t>, const unsigned int*> g_auto_done;
+// Device address of the status word of the last call per (device, stream)
+// that has one (the blocked, next-hop and fp32 sweeps), for fw_check_faults.
+std::map<std::pair<int, cudaStream_t>, unsigned int*> g_last_status;
+
+// Host-side fault injection for tests (fw_debug_inject), per host thread.
+thread_local int t_inject = 0;
 
 // ----------------------------------------------------------------- profiling
 struct ProfState {
@@ -107,8 +113,9 @@ void* workspace_get(cudaStream_t s, size_t bytes) {
         cudaFree(w.ptr);
         w.ptr = nullptr;
         w.bytes = 0;
-        // an FW_VARIANT_AUTO report of this stream pointed into it
+        // an FW_VARIANT_AUTO report and a status word of this stream pointed into it
         g_auto_done.erase({dev, s});
+        g_last_status.erase({dev, s});
     }
     void* p = nullptr;
     const cudaError_t e = cudaMalloc(&p, bytes);
@@ -121,6 +128,54 @@ void* workspace_get(cudaStream_t s, size_t bytes) {
     w.ptr = p;
     w.bytes = bytes;
     return p;
+}
+
+// Zeroes the call's status block on `s` and records its first word as the
+// stream's last status word.
+int status_begin(cudaStream_t s, void* status_block) {
+    FW_CUDA_TRY(cudaMemsetAsync(status_block, 0, kStatusBytes, s));
+    int dev = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ws_mutex);
+    g_last_status[{dev, s}] = static_cast<unsigned int*>(status_block);
+    return FW_OK;
+}
+
+// Test hook: a pending FW_INJECT_CALL_FAULT makes the call's status word
+// nonzero after its kernels, as a missed copy would.
+int status_end(cudaStream_t s, void* status_block) {
+    if (t_inject & FW_INJECT_CALL_FAULT) {
+        t_inject &= ~FW_INJECT_CALL_FAULT;
+        FW_CUDA_TRY(cudaMemsetAsync(status_block, 0x01, 1, s));
+    }
+    return FW_OK;
+}
+
+bool take_packed_fault_injection() {
+    const bool on = (t_inject & FW_INJECT_PACKED_FAULT) != 0;
+    t_inject &= ~FW_INJECT_PACKED_FAULT;
+    return on;
+}
+
+const unsigned int* last_call_status(cudaStream_t s) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_ws_mutex);
+    auto it = g_last_status.find({dev, s});
+    return it == g_last_status.end() ? nullptr : it->second;
+}
+
+void forget_auto_report(cudaStream_t s) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_ws_mutex);
+    g_auto_done.erase({dev, s});
 }
 
 namespace {
@@ -186,10 +241,10 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     (void)tile;
     (void)kappa;
     if (n < 1) return 0;
-    if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
+    if (variant == FW_VARIANT_BASELINE) return kStatusBytes + pivot_workspace_bytes(n);
     const size_t blocked = blocked_workspace_bytes(n, 2);
-    if (variant == FW_VARIANT_AUTO) return ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
-    return blocked;
+    if (variant == FW_VARIANT_AUTO) return kStatusBytes + ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
+    return kStatusBytes + blocked;
 }
 
 }  // extern "C"
@@ -197,10 +252,11 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
 namespace fw {
 size_t min_workspace_bytes(int64_t n, int kappa, int variant) {
     if (n < 1) return 0;
-    if (variant == FW_VARIANT_BASELINE) return pivot_workspace_bytes(n);
+    if (variant == FW_VARIANT_BASELINE) return kStatusBytes + pivot_workspace_bytes(n);
     const size_t blocked = blocked_workspace_bytes(n, blocks_per_pass(variant, kappa, n));
-    if (variant == FW_VARIANT_AUTO) return ((blocked_workspace_bytes(n, 2) + 255) & ~size_t(255)) + p16_workspace_bytes(n);
-    return blocked;
+    if (variant == FW_VARIANT_AUTO)
+        return kStatusBytes + ((blocked_workspace_bytes(n, 2) + 255) & ~size_t(255)) + p16_workspace_bytes(n);
+    return kStatusBytes + blocked;
 }
 }  // namespace fw
 
@@ -218,12 +274,21 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
     if ((reinterpret_cast<uintptr_t>(d_workspace) & 255u) != 0)
         return set_error(FW_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    if (variant == FW_VARIANT_BASELINE) return pivot_solve(d_D, n, d_workspace, s);
-    const int blocks = blocks_per_pass(variant, kappa, n);
-    if (variant == FW_VARIANT_AUTO) {
+    // Layout: the status block (kStatusBytes; its first word counts the
+    // call's missed tile copies), then the sweep's own workspace.
+    void* status = d_workspace;
+    char* body = static_cast<char*>(d_workspace) + kStatusBytes;
+    const size_t body_bytes = workspace_bytes - kStatusBytes;
+    unsigned int* faults = static_cast<unsigned int*>(status);
+    if (int rc = status_begin(s, status)) return rc;
+    int rc = FW_OK;
+    if (variant == FW_VARIANT_BASELINE) {
+        rc = pivot_solve(d_D, n, body, s);
+    } else if (variant == FW_VARIANT_AUTO) {
         const size_t blocked = (blocked_workspace_bytes(n, 2) + 255) & ~size_t(255);
         const unsigned int* done = nullptr;
-        if (int rc = p16_solve(d_D, n, static_cast<char*>(d_workspace) + blocked, s, &done)) return rc;
+        rc = p16_solve(d_D, n, body + blocked, s, &done, take_packed_fault_injection());
+        if (rc) return rc;
         {
             int dev = 0;
             cudaGetDevice(&dev);
@@ -233,9 +298,12 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
         // The int32 fallback behind the flag runs the two-block schedule on
         // one stream: its remainder launches are persistent, so that they
         // cost little when the packed result is taken.
-        return blocked_solve(d_D, n, 2, d_workspace, blocked, s, done);
+        rc = blocked_solve(d_D, n, 2, body, blocked, s, done, faults);
+    } else {
+        rc = blocked_solve(d_D, n, blocks_per_pass(variant, kappa, n), body, body_bytes, s, nullptr, faults);
     }
-    return blocked_solve(d_D, n, blocks, d_workspace, workspace_bytes, s);
+    if (rc) return rc;
+    return status_end(s, status);
 }
 
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {
@@ -245,6 +313,29 @@ int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_st
     void* ws = workspace_get(s, need);
     if (!ws) return FW_ERR_NO_MEMORY;
     return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, ws, need, stream);
+}
+
+int fw_check_faults(fw_stream_t stream, unsigned int* count) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const unsigned int* word = last_call_status(s);
+    if (!word) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_check_faults: no call with a status word on this device "
+                                                         "and stream (or its library workspace was replaced)");
+    FW_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned int v = 0;
+    FW_CUDA_TRY(cudaMemcpy(&v, word, sizeof(v), cudaMemcpyDeviceToHost));
+    if (count) *count = v;
+    if (v)
+        return set_error(FW_ERR_TIMEOUT, std::to_string(v) +
+                                             " tile copies did not arrive within their bounded wait; the call's "
+                                             "result is not valid");
+    return FW_OK;
+}
+
+int fw_debug_inject(int kinds) {
+    if (kinds & ~(FW_INJECT_CALL_FAULT | FW_INJECT_PACKED_FAULT))
+        return set_error(FW_ERR_INVALID_ARGUMENT, "fw_debug_inject: unknown kind " + std::to_string(kinds));
+    t_inject = kinds;
+    return FW_OK;
 }
 
 int fw_apsp_auto_report(fw_stream_t stream, int* used_packed) {
@@ -271,9 +362,13 @@ int fw_apsp_paths_i32(int32_t* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_
     if (n < 1 || n > 65535 || batch < 1 || batch > 65535)
         return set_error(FW_ERR_INVALID_ARGUMENT, "fw_apsp_paths_i32: need 1 <= n <= 65535 and 1 <= batch <= 65535");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    void* ws = workspace_get(s, f32_workspace_bytes(n, batch));
+    void* ws = workspace_get(s, kStatusBytes + f32_workspace_bytes(n, batch));
     if (!ws) return FW_ERR_NO_MEMORY;
-    return i32_paths(d_D, d_nh, n, batch, ws, s);
+    if (int rc = status_begin(s, ws)) return rc;
+    if (int rc = i32_paths(d_D, d_nh, n, batch, static_cast<char*>(ws) + kStatusBytes, s,
+                           static_cast<unsigned int*>(ws)))
+        return rc;
+    return status_end(s, ws);
 }
 
 int fw_path_length_i32(const int32_t* h_nh, int64_t n, int64_t i, int64_t j, int32_t* h_path, int64_t cap) {
@@ -298,10 +393,13 @@ int fw_forward_f32(float* d_D, int32_t* d_nh, int64_t n, int64_t batch, fw_strea
     if (n < 1 || n > 65535 || batch < 1 || batch > 65535)
         return set_error(FW_ERR_INVALID_ARGUMENT, "fw_forward_f32: need 1 <= n <= 65535 and 1 <= batch <= 65535");
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const size_t need = f32_workspace_bytes(n, batch);
-    void* ws = workspace_get(s, need);
+    void* ws = workspace_get(s, kStatusBytes + f32_workspace_bytes(n, batch));
     if (!ws) return FW_ERR_NO_MEMORY;
-    return f32_forward(d_D, d_nh, n, batch, ws, s);
+    if (int rc = status_begin(s, ws)) return rc;
+    if (int rc = f32_forward(d_D, d_nh, n, batch, static_cast<char*>(ws) + kStatusBytes, s,
+                             static_cast<unsigned int*>(ws)))
+        return rc;
+    return status_end(s, ws);
 }
 
 int fw_backward(const float* d_dLdD, const int32_t* d_nh, float* d_dLdW, int64_t n, int64_t batch,
@@ -376,6 +474,11 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count) {
 
 int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream) {
     return measure_relax_peak(dpx_only, mixed, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int fw_measure_int32_rates(double* rates, int count, fw_stream_t stream) {
+    if (!rates || count < 1) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_measure_int32_rates: no output");
+    return measure_int32_rates(rates, count, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int fw_measure_relax_peak_packed(double* dpx_only, double* mixed, fw_stream_t stream) {

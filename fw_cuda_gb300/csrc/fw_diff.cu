@@ -346,24 +346,29 @@ __global__ void __launch_bounds__(kFThreads, 1)
 // pt: tiles (I, J), I from `rows` (nrows), J from `cols` (ncols), one per
 // blockIdx.x; or, with cross >= 0, block pt's update of block u = pt + 1's
 // row and column: tiles [0, T - 1) are (u, J), J != pt, the next T - 2 are
-// (I, u), I != pt, u.
+// (I, u), I != pt, u. A copy that misses its bounded wait is counted in
+// `faults` (the call's status word) and g_nh_copy_faults; the CTA then waits
+// for the copies it issued and leaves its tile as it was.
 template <typename V>
 __global__ void __launch_bounds__(kFThreads, 1)
     fw_nh_remainder_kernel(V* __restrict__ Dall, int* __restrict__ nhall, int64_t n, int pt, int T, TileSet rows,
                            TileSet cols, int ncols, int cross, const __grid_constant__ CUtensorMap mapCT,
-                           const __grid_constant__ CUtensorMap mapCH, const __grid_constant__ CUtensorMap mapRP) {
+                           const __grid_constant__ CUtensorMap mapCH, const __grid_constant__ CUtensorMap mapRP,
+                           unsigned* __restrict__ faults) {
     extern __shared__ __align__(128) int smem[];
     __shared__ __align__(8) uint64_t bars[kFTStages];
     __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     if (tid == 0) {
         s_ok = (smem_u32(smem) & 127u) == 0;
-        if (!s_ok) atomicAdd(&g_nh_copy_faults, 1u);
         for (int i = 0; i < kFTStages; ++i) mbar_init(&bars[i], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    const bool ok = s_ok != 0;
+    if (!s_ok) {  // no copy can be issued: the tile keeps its values
+        if (tid == 0) count_copy_fault(&g_nh_copy_faults, faults);
+        return;
+    }
     const int gph = (int)blockIdx.z;
     V* D = Dall + (int64_t)gph * n * n;
     int* nh = nhall + (int64_t)gph * n * n;
@@ -386,7 +391,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
     // Per slab: the column panel's values and next hops at rows r0.., the row
     // panel's values at columns c0.., by TMA into one stage.
     auto issue = [&](int j) {
-        if (tid == 0 && ok) {
+        if (tid == 0) {
             const int stg = j % kFTStages;
             int* dst = smem + stg * kFStageInts;
             mbar_expect_tx(&bars[stg], (uint32_t)kFStageInts * 4);
@@ -401,20 +406,19 @@ __global__ void __launch_bounds__(kFThreads, 1)
 #pragma unroll
     for (int j = 0; j < kFTStages - 1; ++j)
         if (j < nslab) issue(j);
-    bool arrived = true;
     for (int kb = 0; kb < nslab; ++kb) {
         const int stg = kb % kFTStages;
-        if (ok && !mbar_wait(&bars[stg], (uint32_t)((kb / kFTStages) & 1))) {
-            if (arrived) atomicAdd(&g_nh_copy_faults, 1u);
-            arrived = false;
+        // every thread is past slab kb - 1 (its stage can be refilled), and all
+        // agree whether slab kb arrived
+        if (!ring_wait_all(&bars[stg], (uint32_t)((kb / kFTStages) & 1))) {
+            if (tid == 0) count_copy_fault(&g_nh_copy_faults, faults);
+            ring_drain(bars, kFTStages, kb, min(kb + kFTStages - 2, nslab - 1));
+            return;
         }
-        __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
         if (kb + kFTStages - 1 < nslab) issue(kb + kFTStages - 1);
-        if (ok && arrived) {
-            const int* st = smem + stg * kFStageInts;
-            f_relax_slab<V>(c, h, reinterpret_cast<const V*>(st), st + kFSlabInts,
-                            reinterpret_cast<const V*>(st + 2 * kFSlabInts), min(kSlab, kv - kb * kSlab), tx, ty);
-        }
+        const int* st = smem + stg * kFStageInts;
+        f_relax_slab<V>(c, h, reinterpret_cast<const V*>(st), st + kFSlabInts,
+                        reinterpret_cast<const V*>(st + 2 * kFSlabInts), min(kSlab, kv - kb * kSlab), tx, ty);
     }
     f_store_tile(c, h, D, nh, n, r0, c0, tx, ty);
 }
@@ -477,7 +481,7 @@ size_t f32_workspace_bytes(int64_t n, int64_t batch) {
 // buffer), while the side stream runs block t's bulk remainder (tiles outside
 // both blocks). The chain for block t+1 starts once block t-1's bulk is done.
 template <typename V>
-int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, KernelClass kc) {
+int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, KernelClass kc, unsigned* faults) {
     static PerDeviceOnce attrs;
     if (int rc = once_per_device(attrs, [] {
             FW_CUDA_TRY(
@@ -525,7 +529,7 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
         if (tiles <= 0) return FW_OK;
         const int b = t & 1;
         fw_nh_remainder_kernel<V><<<dim3((unsigned)tiles, 1, nb), kFThreads, kFTSmemBytes, q>>>(
-            D, nh, n, t, T, rows, cols, ncols, cross, mapCT[b], mapCH[b], mapRP[b]);
+            D, nh, n, t, T, rows, cols, ncols, cross, mapCT[b], mapCH[b], mapRP[b], faults);
         FW_LAUNCH_CHECK("fw_nh_remainder_kernel");
         return FW_OK;
     };
@@ -561,12 +565,12 @@ int nh_forward(V* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s
     return FW_OK;
 }
 
-int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
-    return nh_forward<float>(D, nh, n, batch, ws, s, KC_FWD_F32);
+int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, unsigned* faults) {
+    return nh_forward<float>(D, nh, n, batch, ws, s, KC_FWD_F32, faults);
 }
 
-int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s) {
-    return nh_forward<int>(D, nh, n, batch, ws, s, KC_PATHS_I32);
+int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, unsigned* faults) {
+    return nh_forward<int>(D, nh, n, batch, ws, s, KC_PATHS_I32, faults);
 }
 
 int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s) {

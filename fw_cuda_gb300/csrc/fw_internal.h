@@ -72,6 +72,23 @@ enum KernelClass {
 void prof_begin(KernelClass kc, cudaStream_t s);
 void prof_end(KernelClass kc, cudaStream_t s, double relaxations);
 
+// Every workspace of an asynchronous sweep entry point starts with a status
+// block of this size; its first word counts the call's tile copies that
+// missed their bounded wait (fw_check_faults reads it).
+constexpr size_t kStatusBytes = 256;
+
+// Zeroes the status block on `s` and records it as the stream's last one;
+// status_end applies a pending FW_INJECT_CALL_FAULT test injection.
+int status_begin(cudaStream_t s, void* status_block);
+int status_end(cudaStream_t s, void* status_block);
+// Device address of the status word of the last call on (current device, s),
+// or nullptr.
+const unsigned int* last_call_status(cudaStream_t s);
+// Whether a FW_INJECT_PACKED_FAULT test injection is pending (and clears it).
+bool take_packed_fault_injection();
+// Drops the stream's FW_VARIANT_AUTO report (a later call did not run AUTO).
+void forget_auto_report(cudaStream_t s);
+
 // Per-(device, stream) workspace owned by the library: at least `bytes`,
 // 256-byte aligned, kept for later calls. Returns nullptr (and sets the last
 // error) when allocation fails.
@@ -100,25 +117,30 @@ int blocks_per_pass(int variant, int kappa, int64_t n);
 size_t blocked_workspace_bytes(int64_t n, int blocks);
 // `skip`, when not null, is a device flag: nonzero makes every kernel of the
 // sweep return at once (the packed fast path already produced the result).
+// `faults`, when not null, is the call's status word: every tile copy that
+// misses its bounded wait adds one (the result is then not valid).
 // With ws_bytes >= blocked_workspace_bytes(n, 2) the single-block schedule
 // runs with a one-block look-ahead (two panel buffers).
 int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, size_t ws_bytes, cudaStream_t s,
-                  const unsigned int* skip = nullptr);
+                  const unsigned int* skip = nullptr, unsigned int* faults = nullptr);
 // Smallest workspace fw_apsp_i32_ws accepts for these arguments.
 size_t min_workspace_bytes(int64_t n, int kappa, int variant);
 
 // Exact packed 16-bit fast path (fw_packed16.cu).
 size_t p16_workspace_bytes(int64_t n);
-int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag);
+// inject_copy_fault (tests): mark the packed status as if a tile copy had
+// missed its wait, so that the decode refuses and the int32 sweep runs.
+int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag,
+              bool inject_copy_fault = false);
 size_t pivot_workspace_bytes(int64_t n);
 int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
 
 // Differentiable fp32 forward / backward (fw_diff.cu).
 size_t f32_workspace_bytes(int64_t n, int64_t batch);
-int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
+int f32_forward(float* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, unsigned* faults);
 int f32_backward(const float* G, const int* nh, float* dW, int64_t n, int64_t batch, int* d_bad, cudaStream_t s);
 // int32 sweep that also records next hops (same kernels as the fp32 form).
-int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s);
+int i32_paths(int* D, int* nh, int64_t n, int64_t batch, void* ws, cudaStream_t s, unsigned* faults);
 
 // Remainder tile copies of the next-hop forward that missed their bounded
 // wait (fw_diff.cu; part of fw_copy_faults).
@@ -133,6 +155,9 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s);
 
 // Register-only relaxation-rate kernels (fw_peak.cu).
 int measure_relax_peak(double* dpx_only, double* mixed, cudaStream_t s);
+// Per-class int32 rates (fw_measure_int32_rates; kInt32RateCount entries).
+constexpr int kInt32RateCount = 9;
+int measure_int32_rates(double* rates, int count, cudaStream_t s);
 int measure_relax_peak_packed(double* dpx_only, double* mixed, cudaStream_t s);
 
 }  // namespace fw

@@ -125,31 +125,36 @@ __device__ __forceinline__ int64_t skip_gap(int64_t idx, const TileGap& g) { ret
 // whole 128-wide tiles (INF where there is no value); their 32-row slabs
 // arrive by TMA into the 3-stage ring, one mbarrier per stage, the stage and
 // parity count running across the tiles a persistent CTA takes. The main loop
-// is the in-core remainder's.
+// is the in-core remainder's. A copy that misses its bounded wait is counted
+// in `faults` (the call's status word) and g_ooc_copy_faults; the CTA then
+// waits for the copies it issued and leaves that tile and the rest of its
+// share as they were.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads, 2)
     fw_ooc_update_kernel(int* __restrict__ C, int64_t ldc, int64_t M, int64_t N,
                          const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nslab,
-                         TileGap rgap, TileGap cgap, int one) {
+                         TileGap rgap, TileGap cgap, int one, unsigned* __restrict__ faults) {
     extern __shared__ __align__(128) int smem[];
     __shared__ __align__(8) uint64_t bars[kStages];
     __shared__ int s_ok;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     if (tid == 0) {
         s_ok = (smem_u32(smem) & 127u) == 0;
-        if (!s_ok) atomicAdd(&g_ooc_copy_faults, 1u);
         for (int i = 0; i < kStages; ++i) mbar_init(&bars[i], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    const bool ok = s_ok != 0;
+    if (!s_ok) {  // no copy can be issued: the CTA's tiles keep their values
+        if (tid == 0) count_copy_fault(&g_ooc_copy_faults, faults);
+        return;
+    }
     int g = 0;
     const int64_t tn = (N + kTile - 1) / kTile - (cgap.x1 - cgap.x0);
     const int64_t ntiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * tn;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t r0 = skip_gap(t / tn, rgap) * kTile, c0 = skip_gap(t % tn, cgap) * kTile;
         auto issue = [&](int j) {
-            if (tid == 0 && ok) {
+            if (tid == 0) {
                 const int stg = (g + j) % kStages;
                 int* dst = smem + stg * kStageInts;
                 mbar_expect_tx(&bars[stg], (uint32_t)kStageInts * 4);
@@ -162,19 +167,18 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
         for (int j = 0; j < kStages - 1; ++j)
             if (j < nslab) issue(j);
-        bool arrived = true;
         for (int kb = 0; kb < nslab; ++kb) {
             const int stg = (g + kb) % kStages;
-            if (ok && !mbar_wait(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
-                if (arrived) atomicAdd(&g_ooc_copy_faults, 1u);
-                arrived = false;
+            // every thread is past slab kb - 1 (its stage can be refilled), and
+            // all agree whether slab kb arrived
+            if (!ring_wait_all(&bars[stg], (uint32_t)(((g + kb) / kStages) & 1))) {
+                if (tid == 0) count_copy_fault(&g_ooc_copy_faults, faults);
+                ring_drain(bars, kStages, g + kb, g + min(kb + kStages - 2, nslab - 1));
+                return;
             }
-            __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
             if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
-            if (ok && arrived) {
-                const int* st = smem + stg * kStageInts;
-                relax_slab<kOocMixA>(acc, st, st + kSlabInts, tx, ty, one);
-            }
+            const int* st = smem + stg * kStageInts;
+            relax_slab<kOocMixA>(acc, st, st + kSlabInts, tx, ty, one);
         }
         g += nslab;
         ooc_store_acc<VEC>(acc, C, ldc, M, N, r0, c0, tx, ty);
@@ -183,6 +187,11 @@ __global__ void __launch_bounds__(kThreads, 2)
 }
 
 constexpr int kStripeBuffers = 3;
+
+// Adds the status word of one in-core sweep into the call's own.
+__global__ void fw_ooc_add_status_kernel(const unsigned* __restrict__ src, unsigned* __restrict__ dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst += *src;
+}
 
 // Device buffers, streams and events of one call; released by the destructor
 // on every return path.
@@ -195,6 +204,7 @@ struct OocState {
     int* Dg = nullptr;    // w x w: diagonal block, contiguous, closed in place
     int* DgK = nullptr;   // Wp x Wp: Dg* row-major, INF padded
     int* DgT = nullptr;   // Wp x Wp: Dg* transposed, INF padded
+    unsigned* faults = nullptr;  // the call's status word: missed tile copies
     int* buf[kStripeBuffers] = {};
     cudaStream_t in = nullptr, out = nullptr;
     cudaEvent_t ev_in[kStripeBuffers] = {}, ev_comp[kStripeBuffers] = {}, ev_out[kStripeBuffers] = {};
@@ -206,6 +216,7 @@ struct OocState {
         if (out) cudaStreamSynchronize(out);
         for (int* p : {R, R2, CT, CT2, Cst, Dg, DgK, DgT})
             if (p) cudaFree(p);
+        if (faults) cudaFree(faults);
         for (int b = 0; b < kStripeBuffers; ++b) {
             if (buf[b]) cudaFree(buf[b]);
             for (cudaEvent_t e : {ev_in[b], ev_comp[b], ev_out[b]})
@@ -238,8 +249,8 @@ int transpose(const int* src, int64_t lds, int* dst, int64_t ldd, int64_t rows, 
 // A: k-major panel of panel_rows rows, leading dimension lda, of which the
 // a_cols columns from A are valid addresses (the same for B).
 int update(int* C, int64_t ldc, int64_t M, int64_t N, const int* A, int64_t lda, int64_t a_cols, const int* B,
-           int64_t ldb, int64_t b_cols, int64_t panel_rows, int64_t kvalid, int64_t resident, cudaStream_t s,
-           TileGap rgap = {0, 0}, TileGap cgap = {0, 0}) {
+           int64_t ldb, int64_t b_cols, int64_t panel_rows, int64_t kvalid, int64_t resident, unsigned* faults,
+           cudaStream_t s, TileGap rgap = {0, 0}, TileGap cgap = {0, 0}) {
     const int64_t tiles = ((M + kTile - 1) / kTile - (rgap.x1 - rgap.x0)) * ((N + kTile - 1) / kTile - (cgap.x1 - cgap.x0));
     if (tiles <= 0) return FW_OK;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, resident);
@@ -252,10 +263,10 @@ int update(int* C, int64_t ldc, int64_t M, int64_t N, const int* A, int64_t lda,
     prof_begin(KC_OOC_UPDATE, s);
     if (vec)
         fw_ooc_update_kernel<true>
-            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1);
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1, faults);
     else
         fw_ooc_update_kernel<false>
-            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1);
+            <<<grid, kThreads, kSmemBytes, s>>>(C, ldc, M, N, mapA, mapB, nslab, rgap, cgap, 1, faults);
     FW_LAUNCH_CHECK("fw_ooc_update_kernel");
     const double rows = (double)M - std::min<double>((double)M, (double)(rgap.x1 - rgap.x0) * kTile);
     const double cols = (double)N - std::min<double>((double)N, (double)(cgap.x1 - cgap.x0) * kTile);
@@ -320,6 +331,11 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
     if (int rc = alloc(&st.DgT, (size_t)Wp * Wp)) return rc;
     for (int b = 0; b < kStripeBuffers; ++b)
         if (int rc = alloc(&st.buf[b], (size_t)H * n)) return rc;
+    if (cudaMalloc(reinterpret_cast<void**>(&st.faults), sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(FW_ERR_NO_MEMORY, "fw_apsp_i32_host: device allocation of the status word failed");
+    }
+    FW_CUDA_TRY(cudaMemsetAsync(st.faults, 0, sizeof(unsigned), s));
     FW_CUDA_TRY(cudaStreamCreateWithFlags(&st.in, cudaStreamNonBlocking));
     FW_CUDA_TRY(cudaStreamCreateWithFlags(&st.out, cudaStreamNonBlocking));
     for (int b = 0; b < kStripeBuffers; ++b) {
@@ -355,6 +371,10 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
                                       cudaMemcpyDeviceToDevice, s));
         if (int rc = fw_apsp_i32(st.Dg, w, 32, 8, FW_VARIANT_MULTI_LAYER, reinterpret_cast<fw_stream_t>(s)))
             return rc;
+        if (const unsigned* word = last_call_status(s)) {
+            fw_ooc_add_status_kernel<<<1, 32, 0, s>>>(word, st.faults);
+            FW_LAUNCH_CHECK("fw_ooc_add_status_kernel");
+        }
         if (int rc = fill_inf(st.DgK, Wp * Wp, s)) return rc;
         if (int rc = fill_inf(st.DgT, Wp * Wp, s)) return rc;
         FW_CUDA_TRY(cudaMemcpy2DAsync(st.DgK, Wp * sizeof(int), st.Dg, w * sizeof(int), w * sizeof(int), w,
@@ -363,8 +383,10 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
         // Panels: R2 = min(R, Dg* (x) R), CT2 = min(CT, Dg*^T (x) CT).
         FW_CUDA_TRY(cudaMemcpyAsync(st.R2, st.R, sizeof(int) * Wp * ldp, cudaMemcpyDeviceToDevice, s));
         FW_CUDA_TRY(cudaMemcpyAsync(st.CT2, st.CT, sizeof(int) * Wp * ldp, cudaMemcpyDeviceToDevice, s));
-        if (int rc = update(st.R2, ldp, w, n, st.DgT, Wp, Wp, st.R, ldp, ldp, Wp, w, resident, s)) return rc;
-        if (int rc = update(st.CT2, ldp, w, n, st.DgK, Wp, Wp, st.CT, ldp, ldp, Wp, w, resident, s)) return rc;
+        if (int rc = update(st.R2, ldp, w, n, st.DgT, Wp, Wp, st.R, ldp, ldp, Wp, w, resident, st.faults, s))
+            return rc;
+        if (int rc = update(st.CT2, ldp, w, n, st.DgK, Wp, Wp, st.CT, ldp, ldp, Wp, w, resident, st.faults, s))
+            return rc;
         FW_CUDA_TRY(cudaEventRecord(st.ev_panels, s));
         // Stripes.
         for (int64_t r0 = 0; r0 < n; r0 += H, ++stripe_no) {
@@ -380,8 +402,8 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
             const int64_t pr0 = std::max(p0, r0), pr1 = std::min(p0 + w, r0 + h);  // P rows in the stripe
             const TileGap rgap = pr0 < pr1 ? TileGap{(pr0 - r0) / kTile, (pr1 - r0 + kTile - 1) / kTile} : TileGap{0, 0};
             const TileGap cgap{p0 / kTile, (p0 + w + kTile - 1) / kTile};
-            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, ldp - r0, st.R2, ldp, ldp, Wp, w, resident, s,
-                                rgap, cgap))
+            if (int rc = update(st.buf[b], n, h, n, st.CT2 + r0, ldp, ldp - r0, st.R2, ldp, ldp, Wp, w, resident,
+                                st.faults, s, rgap, cgap))
                 return rc;
             // columns of P: the column panel, transposed back
             if (int rc = transpose(st.CT2 + r0, ldp, st.buf[b] + p0, n, w, h, s)) return rc;
@@ -399,6 +421,12 @@ int ooc_solve(int32_t* h_D, int64_t n, int64_t W, int64_t H, cudaStream_t s) {
     }
     FW_CUDA_TRY(cudaStreamWaitEvent(s, st.ev_pass_out, 0));
     FW_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned missed = 0;
+    FW_CUDA_TRY(cudaMemcpy(&missed, st.faults, sizeof(missed), cudaMemcpyDeviceToHost));
+    if (missed)
+        return set_error(FW_ERR_TIMEOUT, "fw_apsp_i32_host: " + std::to_string(missed) +
+                                             " tile copies did not arrive within their bounded wait; the result is "
+                                             "not valid");
     return FW_OK;
 }
 

@@ -480,7 +480,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
 // (32 x 256 words) and one of the row panel (32 x 128 words) land in a
 // shared-memory stage and complete a per-stage mbarrier. Every wait is
 // bounded; a copy that does not arrive sets copy_fault, the packed result is
-// then not taken and the int32 sweep runs.
+// then not taken and the int32 sweep runs. After a miss the CTA issues no
+// further copy, waits (bounded) for the ones it issued and leaves its tile.
 constexpr uint32_t kPStageTx = (uint32_t)kPStageWords * 4;  // bytes per stage
 
 // One tile (r0, w0) of D16 (row r0, word column w0) updated with the 256
@@ -503,9 +504,9 @@ __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_
         mbar_init_fence();
     }
     __syncthreads();
-    const bool ok = s_ok != 0;
+    if (!s_ok) return;
     auto issue = [&](int j) {  // slab j into stage j % kPStages, thread 0 only
-        if (tid == 0 && ok) {
+        if (tid == 0) {
             const int stg = j % kPStages;
             uint32_t* dst = psm + stg * kPStageWords;
             mbar_expect_tx(&bars[stg], kPStageTx);
@@ -517,19 +518,18 @@ __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_
     p_load_tile(c, D16, ldw, r0, w0, tx, ty);
 #pragma unroll
     for (int j = 0; j < kPStages - 1; ++j) issue(j);
-    bool arrived = true;
     for (int kb = 0; kb < nslab; ++kb) {
         const int stg = kb % kPStages;
-        if (ok && !mbar_wait(&bars[stg], (uint32_t)((kb / kPStages) & 1))) {
-            arrived = false;
-            atomicOr(&st->copy_fault, 1u);
+        // every thread is past slab kb - 1 (its stage can be refilled), and all
+        // agree whether slab kb arrived
+        if (!ring_wait_all(&bars[stg], (uint32_t)((kb / kPStages) & 1))) {
+            if (tid == 0) atomicOr(&st->copy_fault, 1u);
+            ring_drain(bars, kPStages, kb, min(kb + kPStages - 2, nslab - 1));
+            return;
         }
-        __syncthreads();  // every thread is past slab kb - 1: its stage can be refilled
         if (kb + kPStages - 1 < nslab) issue(kb + kPStages - 1);
-        if (ok && arrived) {
-            const uint32_t* stage = psm + stg * kPStageWords;
-            p_relax_slab<kP16MixA>(c, stage, stage + kPSlabA, tx, ty, one);
-        }
+        const uint32_t* stage = psm + stg * kPStageWords;
+        p_relax_slab<kP16MixA>(c, stage, stage + kPSlabA, tx, ty, one);
     }
     p_store_tile(c, D16, ldw, r0, w0, tx, ty);
 }
@@ -581,7 +581,8 @@ size_t p16_workspace_bytes(int64_t n) {
 // receives the device address of the word that tells the int32 kernels to
 // skip. The sweep looks one pivot block ahead (two panel buffers): see the
 // schedule below.
-int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag) {
+int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag,
+              bool inject_copy_fault) {
     static PerDeviceOnce attrs;
     if (int rc = once_per_device(attrs, [] {
             FW_CUDA_TRY(
@@ -697,6 +698,7 @@ int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned in
     }
     // The side stream's last launch follows every launch of the chain.
     FW_CUDA_TRY(cudaStreamWaitEvent(s, aux.bulk[(T - 1) & 1], 0));
+    if (inject_copy_fault) FW_CUDA_TRY(cudaMemsetAsync(&st->copy_fault, 0x01, 1, s));
     fw_p16_rmax_kernel<<<cgrid, kCodeThreads, 0, s>>>(D16, n, ld, st);
     FW_LAUNCH_CHECK("fw_p16_rmax_kernel");
     if (vec)

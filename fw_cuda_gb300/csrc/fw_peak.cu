@@ -89,6 +89,78 @@ __global__ void __launch_bounds__(256) fw_peak_packed_kernel(const unsigned* __r
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Instruction-class probes of the int32 relaxation ceiling: each thread keeps
+// 16 independent accumulators and updates every one of them per iteration
+// with operands taken from other accumulators (nothing can be hoisted). OP:
+//   0 DPX add-min            acc = min(x + o, acc)            (1 relaxation)
+//   1 integer multiply-add   acc = o * one + acc
+//   2 DPX three-way min      acc = min(acc, o, p)
+//   3 add                    acc = acc + o
+//   4 min                    acc = min(acc, o)
+//   5 add-min and multiply-add alternating over the accumulators
+//   6 form B (two multiply-adds + one three-way min: 2 relaxations)
+//   7 form A (two DPX add-mins: 2 relaxations)
+//   8 three relaxations: form B, then one DPX add-min
+template <int OP>
+__global__ void __launch_bounds__(256) fw_rate_kernel(const int* __restrict__ in, int* __restrict__ out, int iters,
+                                                      int one) {
+    int acc[16], x[4];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc[i] = in[(threadIdx.x + i) & 255];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) x[i] = in[256 + ((threadIdx.x + i) & 255)];
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int o = acc[(i + 5) & 15];
+            const int p = acc[(i + 11) & 15];
+            if (OP == 0) acc[i] = __viaddmin_s32(x[i & 3], o, acc[i]);
+            if (OP == 1) acc[i] = add_on_fma(o, acc[i], one);
+            if (OP == 2) acc[i] = __vimin3_s32(acc[i], o, p);
+            if (OP == 3) acc[i] = acc[i] + o;
+            if (OP == 4) acc[i] = min(acc[i], o);
+            if (OP == 5) acc[i] = (i & 1) ? add_on_fma(o, acc[i], one) : __viaddmin_s32(x[i & 3], o, acc[i]);
+            if (OP == 6) acc[i] = relax2(false, acc[i], x[i & 3], o, x[(i + 1) & 3], p, one);
+            if (OP == 7) acc[i] = relax2(true, acc[i], x[i & 3], o, x[(i + 1) & 3], p, one);
+            if (OP == 8) acc[i] = __viaddmin_s32(x[(i + 2) & 3], acc[(i + 3) & 15],
+                                                 relax2(false, acc[i], x[i & 3], o, x[(i + 1) & 3], p, one));
+        }
+    }
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s ^= acc[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// Best of five timed launches (after one warm-up) of fw_rate_kernel<OP>;
+// *rate = `per_thread_iter` units per thread-iteration / second.
+template <int OP>
+int time_rate(int blocks, const int* in, int* out, cudaStream_t s, double per_thread_iter, double* rate) {
+    constexpr int kIters = 2048;
+    cudaEvent_t e0, e1;
+    FW_CUDA_TRY(cudaEventCreate(&e0));
+    FW_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 6; ++rep) {
+        cudaEventRecord(e0, s);
+        fw_rate_kernel<OP><<<blocks, 256, 0, s>>>(in, out, kIters, 1);
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_error(e, "fw_rate_kernel");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *rate = (double)blocks * 256.0 * kIters * per_thread_iter / (best * 1e-3);
+    return FW_OK;
+}
+
 template <int MIXA>
 int time_peak(int blocks, const int* in, int* out, cudaStream_t s, double* rate) {
     cudaEvent_t e0, e1;
@@ -169,6 +241,34 @@ int measure_relax_peak_packed(double* dpx_only, double* mixed, cudaStream_t s) {
     double best = r8;
     for (double r : {r6, r5, r4, r3}) best = r > best ? r : best;
     if (mixed) *mixed = best;
+    return FW_OK;
+}
+
+int measure_int32_rates(double* rates, int count, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    FW_CUDA_TRY(cudaGetDevice(&dev));
+    FW_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8;
+    int *in = nullptr, *out = nullptr;
+    FW_CUDA_TRY(cudaMallocAsync(&in, 1024 * sizeof(int), s));
+    FW_CUDA_TRY(cudaMallocAsync(&out, (size_t)blocks * 256 * sizeof(int), s));
+    FW_CUDA_TRY(cudaMemsetAsync(in, 0, 1024 * sizeof(int), s));
+    double r[kInt32RateCount] = {};
+    // instruction classes: lane operations per second (16 per thread-iteration)
+    int rc = time_rate<0>(blocks, in, out, s, 16, &r[0]);
+    if (!rc) rc = time_rate<1>(blocks, in, out, s, 16, &r[1]);
+    if (!rc) rc = time_rate<2>(blocks, in, out, s, 16, &r[2]);
+    if (!rc) rc = time_rate<3>(blocks, in, out, s, 16, &r[3]);
+    if (!rc) rc = time_rate<4>(blocks, in, out, s, 16, &r[4]);
+    if (!rc) rc = time_rate<5>(blocks, in, out, s, 16, &r[5]);
+    // relaxation forms: relaxations per second
+    if (!rc) rc = time_rate<6>(blocks, in, out, s, 32, &r[6]);
+    if (!rc) rc = time_rate<7>(blocks, in, out, s, 32, &r[7]);
+    if (!rc) rc = time_rate<8>(blocks, in, out, s, 48, &r[8]);
+    cudaFreeAsync(in, s);
+    cudaFreeAsync(out, s);
+    if (rc) return rc;
+    for (int i = 0; i < count && i < kInt32RateCount; ++i) rates[i] = r[i];
     return FW_OK;
 }
 

@@ -36,10 +36,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                  : "memory");
 }
 
-// true once the phase with this parity has completed; false after the bound.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// true once the phase with this parity has completed; false after `spins`
+// unsuccessful tries.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int spins = kMbarSpins) {
     const uint32_t addr = smem_u32(bar);
-    for (int i = 0; i < kMbarSpins; ++i) {
+    for (int i = 0; i < spins; ++i) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -49,6 +50,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+
+// One slab wait of a copy ring, agreed by the whole CTA: true only when the
+// slab's copy arrived for every thread (one thread whose bounded wait gave up
+// makes it false for all). It is also the CTA barrier after which the stage
+// of the previous slab may be refilled.
+__device__ __forceinline__ bool ring_wait_all(uint64_t* bar, uint32_t parity) {
+    const bool got = mbar_wait(bar, parity);
+    return __syncthreads_or(got ? 0 : 1) == 0;
+}
+
+// After a missed slab: bounded waits for every copy already issued into the
+// ring (running slab counts first .. last, stage j % stages, phase j / stages),
+// so that no copy is still writing the CTA's shared memory when it stops
+// using the ring. Copies that still do not arrive cannot be waited for longer.
+__device__ __forceinline__ void ring_drain(uint64_t* bars, int stages, int first, int last) {
+    for (int j = first; j <= last; ++j) mbar_wait(&bars[j % stages], (uint32_t)((j / stages) & 1));
+}
+
+// A missed copy: one more in the process-lifetime counter of the translation
+// unit and, when the call has one, in the call's own status word.
+__device__ __forceinline__ void count_copy_fault(unsigned int* process_total, unsigned int* call_word) {
+    atomicAdd(process_total, 1u);
+    if (call_word) atomicAdd(call_word, 1u);
 }
 
 // Box (x, y) of the 2-D map into shared memory (128-byte aligned), completing

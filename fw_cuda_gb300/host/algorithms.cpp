@@ -23,6 +23,13 @@ void run_or_exit(WeightType* d_D, int n, int tileSize, int kappa, int variant, c
                   << ")\n";
         std::exit(EXIT_FAILURE);
     }
+    // A tile copy that missed its bounded wait leaves the result invalid.
+    unsigned int missed = 0;
+    const int fc = fw_check_faults(nullptr, &missed);
+    if (fc != FW_OK) {
+        std::cerr << "fw103 error in " << name << " (status " << fc << "): " << fw_last_error_string() << "\n";
+        std::exit(EXIT_FAILURE);
+    }
 }
 
 }  // namespace

@@ -85,12 +85,16 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
  * whose pool already owns the GPU's free memory, code that must not take the
  * implicit synchronisation of cudaMalloc/cudaFree, a plugin host without an
  * allocator). No counterpart in the reference. The workspace is a fixed
- * 8 MiB array inside the library's device image, held by every GPU that
- * loads the library until exit; n > 8192 is rejected with
- * FW_ERR_INVALID_ARGUMENT. All calls share that array: calls whose GPU work
- * overlaps (other streams, other host threads) race and must be serialised
- * by the caller. The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress); make it before any stream capture. */
+ * array of 8 MiB + 256 bytes inside the library's device image, held by every
+ * GPU that loads the library until exit; n > 8192 is rejected with
+ * FW_ERR_INVALID_ARGUMENT. FW_VARIANT_AUTO runs the int32 multi-layer sweep
+ * here and kappa > 4 runs as kappa 4 (same result; after an AUTO call
+ * fw_apsp_auto_report has no report for the stream). All calls share that
+ * array: calls whose GPU work overlaps (other streams, other host threads)
+ * race and must be serialised by the caller. The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress); make it before
+ * any stream capture. fw_check_faults reads the call's status word, which
+ * lives in the array: check before the next call. */
 int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
 
 /* ---------------------------------------------------------------- out-of-core */
@@ -233,6 +237,40 @@ int fw_mt19937_outputs(uint32_t seed, uint64_t skip, int64_t count, uint32_t* h_
  * affected tiles are then not updated. Synchronous (reads a device word). */
 int fw_copy_faults(unsigned int* count);
 
+/* Synchronises `stream` and reads the status word of the last call on it (on
+ * the current device) among fw_apsp_i32, fw_apsp_i32_ws, fw_apsp_i32_noalloc,
+ * fw_apsp_paths_i32 and fw_forward_f32. Their kernels wait for each tile copy
+ * with a bounded wait; a copy that does not arrive in time is counted in that
+ * word and the affected tiles are left as they were, instead of the kernel
+ * waiting forever. Returns FW_OK when the count is 0, FW_ERR_TIMEOUT (the
+ * call's result is not valid) when it is not, FW_ERR_INVALID_ARGUMENT when no
+ * such call was made on the stream or its library workspace was replaced
+ * since. *count (may be NULL) receives the count. The word lives in the call's
+ * workspace: ask before freeing a caller workspace (fw_apsp_i32_ws).
+ * The reference has no status (it prints and exits on a CUDA error,
+ * include/cuda_utils.cuh:13-32); the C++ shims of fw103_algorithms.h call
+ * this after every solve and keep that print-and-exit contract. */
+int fw_check_faults(fw_stream_t stream, unsigned int* count);
+
+/* Test hooks: host-side fault injection, no GPU fault involved.
+ * FW_INJECT_CALL_FAULT: the next sweep call on this host thread sets its own
+ * status word after its kernels, as one missed tile copy would, so that
+ * fw_check_faults (and the C++ shims) report FW_ERR_TIMEOUT.
+ * FW_INJECT_PACKED_FAULT: the next FW_VARIANT_AUTO call marks its packed
+ * sweep as having missed a copy before the guarded decode, so the packed
+ * result is refused and the int32 sweep produces the result (as it does
+ * after a real miss). Kinds may be OR-ed; 0 clears pending injections. */
+#define FW_INJECT_CALL_FAULT 1
+#define FW_INJECT_PACKED_FAULT 2
+int fw_debug_inject(int kinds);
+
+/* Test hook: one CTA arms an mbarrier for a 16-byte transfer that is never
+ * issued and waits for it with the kernels' bounded wait, limited to `spins`
+ * tries (1 .. 1048576); then it completes the transfer count itself so the
+ * barrier is left balanced. Returns FW_ERR_TIMEOUT when the wait gave up (the
+ * expected outcome), FW_OK if it did not. Synchronous. */
+int fw_debug_bounded_wait(int spins, fw_stream_t stream);
+
 /* Message of the last failure on this host thread ("" if none). */
 const char* fw_last_error_string(void);
 
@@ -261,6 +299,20 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count);
  * relaxation is one DPX add-min instruction (dpx_only), and the best rate of
  * the instruction mix the blocked kernels use (mixed). */
 int fw_measure_relax_peak(double* dpx_only, double* mixed, fw_stream_t stream);
+
+/* What the int32 relaxation rate is built from, measured with register-only
+ * kernels (8 CTAs of 256 threads per SM, 16 independent accumulators per
+ * thread, no memory traffic). rates[0..8] (up to `count` entries):
+ *   lane operations per second of one instruction class alone:
+ *   [0] DPX add-min min(a + b, c)   [1] integer multiply-add a * 1 + b
+ *   [2] DPX three-way min           [3] add             [4] min
+ *   [5] [0] and [1] alternating (both classes counted);
+ *   relaxations per second of a relaxation form:
+ *   [6] two multiply-adds + one three-way min (2 relaxations)
+ *   [7] two DPX add-mins (2 relaxations)
+ *   [8] [6] followed by one DPX add-min (3 relaxations).
+ * No counterpart in the reference. */
+int fw_measure_int32_rates(double* rates, int count, fw_stream_t stream);
 
 /* The same for the packed 16-bit form of FW_VARIANT_AUTO's fast path (two
  * 15-bit lanes per word): every relaxation pair one packed DPX add-min

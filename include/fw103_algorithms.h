@@ -9,8 +9,10 @@
  *   hasNegativeCycle                      src/utils.cpp:5-12
  * The three GPU functions call fw_apsp_i32 (fw103.h) on the legacy default
  * stream and return after cudaDeviceSynchronize, like the reference's
- * launchers; on a nonzero status they print the error and exit(EXIT_FAILURE),
- * like the reference's checkCudaErrors (include/cuda_utils.cuh:13-32).
+ * launchers; on a nonzero status (of the call, of the synchronisation, or of
+ * fw_check_faults: a tile copy that missed its bounded wait) they print the
+ * error and exit(EXIT_FAILURE), like the reference's checkCudaErrors
+ * (include/cuda_utils.cuh:13-32).
  * All of it is exported by libfw103.so.
  */
 #ifndef FW103_ALGORITHMS_H

@@ -40,7 +40,10 @@ def build() -> None:
     """Compile the oracle's own sources (and, where the reference checkout
     exists, the reference CPU library and kernel cubins)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_root = os.environ.get("FW_REFERENCE_ROOT", "/root/reference")
+    # The reference checkout: FW_REFERENCE_ROOT, else a directory named
+    # `reference` beside this repository.
+    ref_root = os.environ.get("FW_REFERENCE_ROOT",
+                              os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
     if os.path.isdir(os.path.join(ref_root, "src")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
 

@@ -57,3 +57,37 @@ def test_clock_summary_flags_throttling():
     assert r["samples"] == 3 and r["sm_max_mhz"] == 2070.0 and r["sm_mhz"] == 2065.0 and r["sm_mhz_min"] == 1800.0
     assert r["reasons"] == ["hw_slowdown", "sw_power_cap"]
     assert bench.ClockSampler(0).summary()["samples"] == 0
+
+
+class _FakeRates:
+    """Stands in for the library's probe entry points (no GPU here)."""
+
+    def measure_relax_peak(self, stream):
+        return 1.9e13, 2.0e13
+
+    def measure_int32_rates(self, stream):
+        return {"dpx_addmin": 1.9e13, "imad": 1.9e13, "dpx_min3": 1.9e13, "add": 3.2e13, "min": 1.9e13,
+                "dpx_addmin_imad_alternating": 2.8e13, "form_b_relax": 1.75e13, "form_a_relax": 1.91e13,
+                "form_b_then_addmin_relax": 2.0e13}
+
+
+def test_int32_ceiling_model():
+    c = bench.int32_ceiling(_FakeRates(), None, None)
+    assert c["peak"] == pytest.approx(2.0e13) and c["peak_form"] in ("form_b_then_addmin_relax", "mixed_probe")
+    # ALU bound r_alu / ((1 + x) / 2) meets the joint bound r_both / ((3 - x) / 2)
+    x = (3 * 1.9 - 2.8) / (1.9 + 2.8)
+    assert c["model_addmin_fraction"] == pytest.approx(x, abs=2e-3)
+    assert c["model_peak"] == pytest.approx(1.9e13 / ((1 + x) / 2), rel=2e-3)
+    assert "per_clock_per_sm" not in c
+
+
+def test_dijkstra_rows_checker(oracle):
+    n = 64
+    W = oracle.generate_graph(n, 0.3, 5, 1, 100)
+    D = oracle.fw_i32(W)
+    rows = {s: D[s].copy() for s in (0, 17, n - 1)}
+    r = bench.dijkstra_rows(W, rows, 2)
+    assert r["rows_vs_dijkstra"] == "3/3" and r["all_rows_match"] and r["rows"] == [0, 17, n - 1]
+    rows[17][3] += 1  # a wrong entry in the result under test is caught
+    r = bench.dijkstra_rows(W, rows, 2)
+    assert r["rows_vs_dijkstra"] == "2/3" and not r["all_rows_match"]

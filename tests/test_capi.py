@@ -90,15 +90,35 @@ def test_host_solve_arguments(fw):
 
 
 def test_workspace_sizes(fw):
-    # blocked: two buffers of two 128-row panels (look-ahead or the two-block
-    # pass), leading dimension padded to 128
-    assert fw.workspace_bytes_i32(1, variant=1) == 2 * 256 * 128 * 4
-    assert fw.workspace_bytes_i32(32768, variant=2) == 2 * 256 * 32768 * 4
-    assert fw.workspace_bytes_i32(32769, variant=2) == 2 * 256 * (32768 + 128) * 4
-    assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == 2 * 256 * 32768 * 4
+    # every workspace starts with a 256-byte status block (the call's missed
+    # copy count); blocked: two buffers of two 128-row panels (look-ahead or
+    # the two-block pass), leading dimension padded to 128
+    status = 256
+    assert fw.workspace_bytes_i32(1, variant=1) == status + 2 * 256 * 128 * 4
+    assert fw.workspace_bytes_i32(32768, variant=2) == status + 2 * 256 * 32768 * 4
+    assert fw.workspace_bytes_i32(32769, variant=2) == status + 2 * 256 * (32768 + 128) * 4
+    assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == status + 2 * 256 * 32768 * 4
     # per-pivot: two row and two column snapshots
-    assert fw.workspace_bytes_i32(1001, variant=0) == 4 * 1004 * 4
+    assert fw.workspace_bytes_i32(1001, variant=0) == status + 4 * 1004 * 4
     assert fw.workspace_bytes_i32(0, variant=1) == 0
+
+
+def test_fault_hooks_reject_bad_arguments(fw):
+    L = fw.lib()
+    assert L.fw_debug_inject(4) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"unknown kind" in L.fw_last_error_string()
+    assert L.fw_debug_inject(0) == fw.FW_OK
+    for spins in (0, -1, (1 << 20) + 1):
+        assert L.fw_debug_bounded_wait(spins, None) == fw.FW_ERR_INVALID_ARGUMENT
+        assert b"spins" in L.fw_last_error_string()
+
+
+def test_noalloc_rejects_before_device_work(fw):
+    L = fw.lib()
+    fake = 0x7F0000000000  # never dereferenced: the size check fails first
+    assert L.fw_apsp_i32_noalloc(fake, 8193, 32, 4, 2, None) == fw.FW_ERR_INVALID_ARGUMENT
+    assert b"8192" in L.fw_last_error_string()
+    assert L.fw_apsp_i32_noalloc(None, 100, 32, 4, 2, None) == fw.FW_ERR_INVALID_ARGUMENT
 
 
 def test_generator_matches_reference_hashes(fw, oracle):

@@ -153,8 +153,9 @@ def test_workspace_variant_matches(fw, cuda, oracle):
     ref = oracle.fw_i32(W)
     need = fw.workspace_bytes_i32(n, variant=2)
     ws = cuda.empty(need // 4 + 64, dtype=cuda.int32, device="cuda")
-    # full size: look-ahead schedule; half: the minimum, one panel buffer
-    for nbytes in (need, need // 2):
+    # full size: look-ahead schedule; the 256-byte status block and one panel
+    # buffer: the minimum
+    for nbytes in (need, 256 + (need - 256) // 2):
         for v in (1, 2):
             d = cuda.from_numpy(W).cuda()
             fw.apsp_i32_ws(d, n, ws, nbytes, variant=v)
