@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     int acc[8][8];
     if (blockIdx.y == 0) {
         load_acc<VEC>(acc, D, n, p0, q0, tx, ty);
-        mainloop<kMixA>(
+        mainloop<kColsA>(
             acc, nslab, smem,
             [&](int* dst, int s) { load_kmajor_async(dst, colT, ldp, s * kSlab, p0, tid); },
             [&](int* dst, int s) { load_d_rows<VEC>(dst, D, n, p0 + s * kSlab, q0, tid); }, tx, ty, one);
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         store_acc_ws(acc, rowP, ldp, q0, tx, ty);
     } else {
         load_acc<VEC>(acc, D, n, q0, p0, tx, ty);
-        mainloop<kMixA>(
+        mainloop<kColsA>(
             acc, nslab, smem,
             [&](int* dst, int s) { load_d_transposed<VEC>(dst, D, n, q0, p0 + s * kSlab, tid); },
             [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldp, s * kSlab, p0, tid); }, tx, ty, one);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
             if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
             const int* st = smem + stg * kStageInts;
-            relax_slab<kMixA>(acc, st, st + kSlabInts, tx, ty, one);
+            relax_slab<kColsA>(acc, st, st + kSlabInts, tx, ty, one);
         }
         g += nslab;
         store_acc<VEC>(acc, D, n, r0, c0, tx, ty);

@@ -42,9 +42,9 @@ namespace {
 
 constexpr int kBuckets = 5;
 constexpr int kBatchMaxN = 4096;
-// Instruction mix of the per-CTA sweep (see kMixA), chosen apart from the
+// Form-A columns of the per-CTA sweep (see kColsA), chosen apart from the
 // TMA-fed remainder's because its slabs arrive by cp.async.
-constexpr int kBatchedMixA = 5;
+constexpr unsigned kBatchedColsA = cols_below(5);
 
 struct BatchItem {
     int64_t offset;
@@ -196,7 +196,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int6
             if (tj == pt) continue;
             const int64_t q0 = (int64_t)tj * kTile;
             load_acc<VEC>(acc, Gm, ldg, p0, q0, tx, ty);
-            mainloop<kBatchedMixA>(
+            mainloop<kBatchedColsA>(
                 acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, p0, tid); },
                 [&](int* dst, int s) { load_d_rows<VEC>(dst, Gm, ldg, p0 + s * kSlab, q0, tid); }, tx, ty, one);
             store_acc<VEC>(acc, Gm, ldg, p0, q0, tx, ty);
@@ -208,7 +208,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int6
             if (ti == pt) continue;
             const int64_t r0 = (int64_t)ti * kTile;
             load_acc<VEC>(acc, Gm, ldg, r0, p0, tx, ty);
-            mainloop<kBatchedMixA>(
+            mainloop<kBatchedColsA>(
                 acc, nslab, smem,
                 [&](int* dst, int s) { load_d_transposed<VEC>(dst, Gm, ldg, r0, p0 + s * kSlab, tid); },
                 [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, p0, tid); }, tx, ty, one);
@@ -224,7 +224,7 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int6
                 if (tj == pt) continue;
                 const int64_t q0 = (int64_t)tj * kTile;
                 load_acc<VEC>(acc, Gm, ldg, r0, q0, tx, ty);
-                mainloop<kBatchedMixA>(
+                mainloop<kBatchedColsA>(
                     acc, nslab, smem, [&](int* dst, int s) { load_kmajor_async(dst, colT, ldw, s * kSlab, r0, tid); },
                     [&](int* dst, int s) { load_kmajor_async(dst, rowP, ldw, s * kSlab, q0, tid); }, tx, ty, one);
                 store_acc<VEC>(acc, Gm, ldg, r0, q0, tx, ty);

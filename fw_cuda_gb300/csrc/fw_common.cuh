@@ -28,12 +28,17 @@ constexpr int kSlabInts = kSlab * kTile;                 // one operand slab
 constexpr int kStageInts = 2 * kSlabInts;                // A slab + B slab
 constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 
-// Number of the 8 micro-tile columns that fold a pivot pair with two DPX
-// add-min instructions; the other columns use form B (see relax2). Measured on
-// GB300 with the TMA-fed remainder kernel (whole multi-layer solve, kappa 8,
-// n = 32768): 8 of 8 (DPX only) 1975 ms, 7 of 8 1918, 6 of 8 1797, 5 of 8
-// 1806, 4 of 8 1807, 3 of 8 1715, 2 of 8 1846, 1 of 8 2045 ms.
-constexpr int kMixA = 3;
+// The micro-tile columns (bit c = column c of the 8) that fold a pivot pair
+// with two DPX add-min instructions (form A); the other columns use form B
+// (see relax2). Measured on GB300 with the TMA-fed remainder kernel: first,
+// whole multi-layer solves (kappa 8, n = 32768) with the first k columns in
+// form A: 8 of 8 (DPX only) 1975 ms, 7 of 8 1918, 6 of 8 1797, 5 of 8 1806,
+// 4 of 8 1807, 3 of 8 1715, 2 of 8 1846, 1 of 8 2045 ms; then all 56 sets of
+// three columns on one remainder launch (n = 16384, 256 pivots): {0, 3, 5}
+// 3.25 ms, {0, 1, 2} 3.37 ms, the slowest set 3.58 ms (which columns take
+// form A changes how the compiler interleaves the two pipes).
+constexpr unsigned cols_below(int k) { return (1u << k) - 1u; }
+constexpr unsigned kColsA = (1u << 0) | (1u << 3) | (1u << 5);
 
 // Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
 // ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns
@@ -63,15 +68,15 @@ __device__ __forceinline__ int relax2(bool form_a, int acc, int a0, int b0, int 
     }
 }
 
-// One pivot pair of the 8 x 8 micro-tile update; columns below MIXA use form A.
-template <int MIXA>
+// One pivot pair of the 8 x 8 micro-tile update; the columns in COLS use form A.
+template <unsigned COLS>
 __device__ __forceinline__ void relax_tile_pair(int (&acc)[8][8], const int (&a0)[8], const int (&b0)[8],
                                                 const int (&a1)[8], const int (&b1)[8], int one) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            acc[r][c] = relax2(c < MIXA, acc[r][c], a0[r], b0[c], a1[r], b1[c], one);
+            acc[r][c] = relax2(((COLS >> c) & 1u) != 0, acc[r][c], a0[r], b0[c], a1[r], b1[c], one);
         }
     }
 }
@@ -92,14 +97,14 @@ __device__ __forceinline__ void load_frag(const int* As, const int* Bs, int kk, 
 
 // acc = min(acc, A (x) B) over one slab of kSlab pivots held in shared memory
 // (A k-major [kSlab][128], B k-major [kSlab][128]).
-template <int MIXA>
+template <unsigned COLS>
 __device__ __forceinline__ void relax_slab(int (&acc)[8][8], const int* As, const int* Bs, int tx, int ty, int one) {
 #pragma unroll 1
     for (int kk = 0; kk < kSlab; kk += 2) {
         int a0[8], b0[8], a1[8], b1[8];
         load_frag(As, Bs, kk, tx, ty, a0, b0);
         load_frag(As, Bs, kk + 1, tx, ty, a1, b1);
-        relax_tile_pair<MIXA>(acc, a0, b0, a1, b1, one);
+        relax_tile_pair<COLS>(acc, a0, b0, a1, b1, one);
     }
 }
 

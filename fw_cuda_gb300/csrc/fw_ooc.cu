@@ -40,8 +40,8 @@ __device__ unsigned int g_ooc_copy_faults = 0;
 
 namespace {
 
-// Instruction mix of the stripe update (see kMixA).
-constexpr int kOocMixA = 5;
+// Form-A columns of the stripe update (see kColsA).
+constexpr unsigned kOocColsA = cols_below(5);
 
 __global__ void fw_ooc_fill_kernel(int* __restrict__ p, int64_t count) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
             if (kb + kStages - 1 < nslab) issue(kb + kStages - 1);
             const int* st = smem + stg * kStageInts;
-            relax_slab<kOocMixA>(acc, st, st + kSlabInts, tx, ty, one);
+            relax_slab<kOocColsA>(acc, st, st + kSlabInts, tx, ty, one);
         }
         g += nslab;
         ooc_store_acc<VEC>(acc, C, ldc, M, N, r0, c0, tx, ty);

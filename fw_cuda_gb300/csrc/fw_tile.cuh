@@ -140,7 +140,7 @@ __device__ __forceinline__ void store_acc_ws_transposed(const int (&acc)[8][8], 
 // (The panel kernels and the batched kernel use it; the remainder kernels
 // stream their slabs by TMA instead.)
 // la(dst, s) / lb(dst, s) fill slab s of A / B (asynchronously or not).
-template <int MIXA, class LA, class LB>
+template <unsigned COLS, class LA, class LB>
 __device__ __forceinline__ void mainloop(int (&acc)[8][8], int nslab, int* smem, LA la, LB lb, int tx, int ty,
                                          int one) {
 #pragma unroll
@@ -162,7 +162,7 @@ __device__ __forceinline__ void mainloop(int (&acc)[8][8], int nslab, int* smem,
         }
         cp_async_commit();
         const int* st = smem + (kb % kStages) * kStageInts;
-        relax_slab<MIXA>(acc, st, st + kSlabInts, tx, ty, one);
+        relax_slab<COLS>(acc, st, st + kSlabInts, tx, ty, one);
     }
 }
 

@@ -121,8 +121,64 @@ def test_batch_equals_single_graphs(cuda):
         assert cuda.allclose(dW1, dWb[b], rtol=1e-5, atol=1e-5)
 
 
+def test_gradient_matches_central_differences_n96(cuda, oracle):
+    """The same check on a larger graph (n = 96): 400 sampled edges, every
+    edge with a nonzero gradient among them weighted in, central differences
+    in FP64 through the oracle sweep, 1e-3 relative."""
+    from fw_cuda_gb300 import autograd as A
+
+    rng = np.random.default_rng(96)
+    n = 96
+    W = workloads.diff_graph(n, rng)
+    G = rng.standard_normal((n, n))
+    Wt = cuda.from_numpy(W).cuda().requires_grad_(True)
+    A.shortest_paths(Wt).backward(cuda.from_numpy(G.astype(np.float32)).cuda())
+    grad = Wt.grad.cpu().numpy().astype(np.float64)
+    W64 = W.astype(np.float64)
+    eps = 1e-3
+
+    def loss(Wp):
+        Dp, _ = oracle.fw_f64_nexthop(Wp)
+        fin = np.isfinite(Dp)
+        return float(np.sum(G[fin] * Dp[fin]))
+
+    edges = [(u, v) for u in range(n) for v in range(n) if u != v and np.isfinite(W64[u, v])]
+    on_paths = [e for e in edges if grad[e] != 0]
+    off_paths = [e for e in edges if grad[e] == 0]
+    assert len(on_paths) > 200
+    pick = [on_paths[i] for i in rng.choice(len(on_paths), 300, replace=False)]
+    pick += [off_paths[i] for i in rng.choice(len(off_paths), 100, replace=False)]
+    for u, v in pick:
+        Wp, Wm = W64.copy(), W64.copy()
+        Wp[u, v] += eps
+        Wm[u, v] -= eps
+        fd = (loss(Wp) - loss(Wm)) / (2 * eps)
+        assert abs(fd - grad[u, v]) <= 1e-3 * max(1.0, abs(fd)), (u, v, fd, grad[u, v])
+
+
+def test_batch_workload_against_fp64_sweep(cuda, oracle):
+    """The differentiable workload's batch, 256 graphs at n = 256: every
+    graph's distances within ULP_TOL of the FP64 sweep with the same k-order,
+    and the batched backward equal to the oracle's path-walk gradient."""
+    from fw_cuda_gb300 import autograd as A
+
+    rng = np.random.default_rng(5)  # the benchmark's batch
+    Ws = np.stack([workloads.diff_graph(256, rng) for _ in range(256)])
+    D, nh = A.forward_with_next_hops(cuda.from_numpy(Ws).cuda())
+    G = np.random.default_rng(6).standard_normal(Ws.shape).astype(np.float32)
+    dW, bad = A.backward_from_next_hops(cuda.from_numpy(G).cuda(), nh, check_walks=True)
+    assert bad == 0
+    D, nh, dW = D.cpu().numpy(), nh.cpu().numpy(), dW.cpu().numpy().astype(np.float64)
+    for b in range(Ws.shape[0]):
+        D64, _ = oracle.fw_f64_nexthop(Ws[b].astype(np.float64))
+        assert ulp_distance(D[b], D64) <= ULP_TOL, b
+        ref, bad_cpu = oracle.fw_backward(G[b].astype(np.float64), nh[b])
+        assert bad_cpu == 0
+        assert np.allclose(dW[b], ref, rtol=1e-5, atol=1e-4), b
+
+
 def test_large_graph_rows_against_dijkstra(cuda):
-    """n = 4096 (the differentiable workload's large graph): sampled rows
+    """n = 4096 (the differentiable workload's large graph): 64 sampled rows
     against FP64 Dijkstra, every walk ends, and the backward runs clean."""
     sp = pytest.importorskip("scipy.sparse.csgraph")
     from fw_cuda_gb300 import autograd as A
@@ -137,7 +193,8 @@ def test_large_graph_rows_against_dijkstra(cuda):
     Dh = D.cpu().numpy()
     W64 = np.where(np.isfinite(W), W, 0.0).astype(np.float64)  # csgraph: 0 = no edge
     np.fill_diagonal(W64, 0.0)
-    rows = [0, 1, 2047, 4095]
+    rows = sorted({0, 1, 2047, 4095, *[int(x) for x in rng.choice(n, 60, replace=False)]})
+    assert len(rows) >= 64
     ref = sp.dijkstra(W64, directed=True, indices=rows)
     for q, i in enumerate(rows):
         ref_row = ref[q].copy()
