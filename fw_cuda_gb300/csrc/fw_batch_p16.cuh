@@ -1,0 +1,400 @@
+// Exact packed 16-bit blocked sweep of one graph by one CTA, for the batched
+// path (fw_batched.cu). The single-graph form is fw_packed16.cu; the argument
+// for exactness is the same, taken per graph:
+//
+//   CAP = 32767. A graph qualifies when every entry is INF or an integer in
+//   [0, CAP). Entries are encoded as themselves, INF as CAP, two per 32-bit
+//   word; packed sums of two encoded values stay below 65535, so every value
+//   the sweep computes is min(CAP, d) with d the true shortest-path length
+//   (non-negative weights: a path shorter than CAP has only shorter
+//   prefixes). Below CAP the results are exact; a CAP entry is INF unless a
+//   finite d >= CAP exists, and then some vertex u on that path has
+//   d(i, u) in [CAP - w_max, CAP). So when the largest result below CAP is
+//   below CAP - w_max (w_max the largest finite entry), decoding CAP -> INF
+//   gives the int32 sweep's result (src/fw_baseline_cpu.cpp:6-15) bit for
+//   bit; otherwise the graph is left untouched and handed to the int32 path.
+//
+// The CTA (256 threads) keeps the graph's 16-bit copy W (leading dimension
+// ld = n rounded up to 128 values, padded with CAP) in its workspace slice,
+// with the current pivot block's panels: colD[k][i] = D[i][p0 + k] duplicated
+// into both halves of a word (the A operand of the packed add-min), rowP[k][*]
+// = row p0 + k as packed words (the B operand). Per 128-wide pivot block:
+// the closure of the diagonal block in registers, the row panel min(R, Dg* x R)
+// and the column panel min(C, C x Dg*) (plain min-plus products, Dg* being
+// closed), then the remainder min(D, C x R), tile after tile. A tile is 128
+// rows x 128 values = 64 words; each thread holds 8 rows x 4 words (16 bytes
+// per row) and folds pivot pairs as the single-graph kernels do: two packed
+// DPX add-mins (form A) or two 32-bit multiply-adds by a runtime 1 on the FMA
+// pipe plus one packed three-way DPX min (form B; exact because every half is
+// at most CAP, so no carry crosses into the other half).
+#pragma once
+
+#include <cstdint>
+
+#include "fw_common.cuh"
+#include "fw_tile.cuh"
+
+namespace fw {
+
+constexpr uint32_t kQCap = 0x7FFF;
+constexpr int kQMaxN = 1024;                          // largest graph the packed batched path takes
+constexpr int kQTileW = kTile / 2;                    // tile width in words
+constexpr int kQSlabA = kSlab * kTile;                // words: 32 pivots x 128 rows (duplicated values)
+constexpr int kQSlabB = kSlab * kQTileW;              // words: 32 pivots x 64 words
+constexpr int kQStageWords = kQSlabA + kQSlabB;
+constexpr int kQSmemBytes = kStages * kQStageWords * 4;  // 72 KB
+// Words (bit w of the thread's 4) that take form A.
+constexpr unsigned kQWordsA = 0x5u;
+
+// Workspace words of one CTA for graphs up to `ld` values wide (ld a
+// multiple of 128): W, colD (128 x ld), rowP (128 x ld / 2).
+__host__ __device__ inline int64_t q_ws_words(int64_t ld) { return ld * (ld / 2) + (int64_t)kTile * ld + (int64_t)kTile * (ld / 2); }
+
+__device__ __forceinline__ uint32_t q_dup(uint32_t v) { return v | (v << 16); }
+
+// Two pivots folded into one packed accumulator word.
+__device__ __forceinline__ uint32_t q_relax2(bool form_a, uint32_t acc, uint32_t a0, uint32_t b0, uint32_t a1,
+                                             uint32_t b1, int one) {
+    if (form_a) return __viaddmin_u16x2(a1, b1, __viaddmin_u16x2(a0, b0, acc));
+    const uint32_t s0 = (uint32_t)add_on_fma((int)a0, (int)b0, one);
+    const uint32_t s1 = (uint32_t)add_on_fma((int)a1, (int)b1, one);
+    return __vimin3_u16x2(acc, s0, s1);
+}
+
+// acc = min(acc, A (x) B) over one 32-pivot slab in shared memory: A k-major
+// [32][128] duplicated words (rows of the tile), B k-major [32][64] words.
+__device__ __forceinline__ void q_relax_slab(uint32_t (&c)[8][4], const uint32_t* As, const uint32_t* Bs, int tx,
+                                             int ty, int one) {
+#pragma unroll 1
+    for (int kk = 0; kk < kSlab; kk += 2) {
+        uint32_t a0[8], a1[8], b0[4], b1[4];
+        {
+            const uint4 l0 = *reinterpret_cast<const uint4*>(As + kk * kTile + ty * 4);
+            const uint4 h0 = *reinterpret_cast<const uint4*>(As + kk * kTile + 64 + ty * 4);
+            const uint4 l1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + ty * 4);
+            const uint4 h1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + 64 + ty * 4);
+            const uint4 q0 = *reinterpret_cast<const uint4*>(Bs + kk * kQTileW + tx * 4);
+            const uint4 q1 = *reinterpret_cast<const uint4*>(Bs + (kk + 1) * kQTileW + tx * 4);
+            a0[0] = l0.x; a0[1] = l0.y; a0[2] = l0.z; a0[3] = l0.w;
+            a0[4] = h0.x; a0[5] = h0.y; a0[6] = h0.z; a0[7] = h0.w;
+            a1[0] = l1.x; a1[1] = l1.y; a1[2] = l1.z; a1[3] = l1.w;
+            a1[4] = h1.x; a1[5] = h1.y; a1[6] = h1.z; a1[7] = h1.w;
+            b0[0] = q0.x; b0[1] = q0.y; b0[2] = q0.z; b0[3] = q0.w;
+            b1[0] = q1.x; b1[1] = q1.y; b1[2] = q1.z; b1[3] = q1.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
+                c[r][w] = q_relax2(((kQWordsA >> w) & 1u) != 0, c[r][w], a0[r], b0[w], a1[r], b1[w], one);
+    }
+}
+
+// The thread's 8 rows x 4 words of the tile at (r0, word w0) of a packed
+// matrix with `ldw` words per row.
+__device__ __forceinline__ void q_load_tile(uint32_t (&c)[8][4], const uint32_t* Wm, int64_t ldw, int64_t r0,
+                                            int64_t w0, int tx, int ty) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const uint4 t = *reinterpret_cast<const uint4*>(Wm + (r0 + own_row(ty, r)) * ldw + w0 + tx * 4);
+        c[r][0] = t.x; c[r][1] = t.y; c[r][2] = t.z; c[r][3] = t.w;
+    }
+}
+
+__device__ __forceinline__ void q_store_tile(const uint32_t (&c)[8][4], uint32_t* Wm, int64_t ldw, int64_t r0,
+                                             int64_t w0, int tx, int ty) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+        *reinterpret_cast<uint4*>(Wm + (r0 + own_row(ty, r)) * ldw + w0 + tx * 4) =
+            make_uint4(c[r][0], c[r][1], c[r][2], c[r][3]);
+}
+
+// k-major slab [32][width] words from rows k0.. of a buffer with `ld` words
+// per row, columns c0.. (16-byte aligned), by cp.async.
+template <int WIDTH>
+__device__ __forceinline__ void q_load_kmajor_async(uint32_t* dst, const uint32_t* buf, int64_t ld, int k0, int64_t c0,
+                                                    int tid) {
+    constexpr int kVecs = kSlab * WIDTH / 4;
+#pragma unroll
+    for (int q = tid; q < kVecs; q += kThreads) {
+        const int row = q / (WIDTH / 4), ch = q % (WIDTH / 4);
+        cp_async16(dst + row * WIDTH + ch * 4, buf + (int64_t)(k0 + row) * ld + c0 + ch * 4);
+    }
+}
+
+// A slab of the column panel taken from the tile itself: dst[kk][i] =
+// dup(value (r0 + i, p0 + k0 + kk)) for kk < 32, i < 128 (plain loads: each
+// thread reads 8 words of one row and writes 16 duplicated values).
+__device__ __forceinline__ void q_load_transposed_dup(uint32_t* dst, const uint32_t* Wm, int64_t ldw, int64_t r0,
+                                                      int64_t pw0, int tid) {
+    const int i = tid & (kTile - 1), part = tid >> 7;  // 2 threads per row, 8 words each
+    const uint32_t* src = Wm + (r0 + i) * ldw + pw0 + part * 8;
+    const uint4 x = *reinterpret_cast<const uint4*>(src);
+    const uint4 y = *reinterpret_cast<const uint4*>(src + 4);
+    const uint32_t v[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        const int kk = part * 16 + 2 * w;
+        dst[kk * kTile + i] = q_dup(v[w] & 0xFFFFu);
+        dst[(kk + 1) * kTile + i] = q_dup(v[w] >> 16);
+    }
+}
+
+// Three-stage cp.async pipeline over `nslab` slabs (the int32 mainloop's
+// schedule); la / lb fill slab s of A / B.
+template <class LA, class LB>
+__device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, uint32_t* smem, LA la, LB lb, int tx,
+                                           int ty, int one) {
+#pragma unroll
+    for (int s = 0; s < kStages - 1; ++s) {
+        if (s < nslab) {
+            la(smem + s * kQStageWords, s);
+            lb(smem + s * kQStageWords + kQSlabA, s);
+        }
+        cp_async_commit();
+    }
+    for (int kb = 0; kb < nslab; ++kb) {
+        cp_async_wait<kStages - 2>();
+        __syncthreads();
+        const int nxt = kb + kStages - 1;
+        if (nxt < nslab) {
+            uint32_t* st = smem + (nxt % kStages) * kQStageWords;
+            la(st, nxt);
+            lb(st + kQSlabA, nxt);
+        }
+        cp_async_commit();
+        const uint32_t* st = smem + (kb % kStages) * kQStageWords;
+        q_relax_slab(c, st, st + kQSlabA, tx, ty, one);
+    }
+    cp_async_wait<0>();
+}
+
+// Publishes pivot k (k & 7 == U, so the thread's register row and word are
+// compile-time) of the block held as c: row k into prow (64 words), column k
+// duplicated into pcol (128 words).
+template <int U>
+__device__ __forceinline__ void q_publish(const uint32_t (&c)[8][4], int k, uint32_t* prow, uint32_t* pcol, int tx,
+                                          int ty) {
+    constexpr int lo = U & 3;          // row k within its group of four rows
+    constexpr int w = (U >> 1) & 3;    // the word of column k among the thread's four
+    constexpr int sh = (U & 1) * 16;   // the half of that word
+    if (ty == ((k & 63) >> 2)) {       // row k = own_row(ty, lo + 4 * (k >> 6))
+        const bool hi = (k >> 6) != 0;
+        *reinterpret_cast<uint4*>(prow + tx * 4) =
+            make_uint4(hi ? c[4 + lo][0] : c[lo][0], hi ? c[4 + lo][1] : c[lo][1], hi ? c[4 + lo][2] : c[lo][2],
+                       hi ? c[4 + lo][3] : c[lo][3]);
+    }
+    if (tx == (k >> 3)) {  // column k = value 2 * (tx * 4 + w) + U % 2
+        uint32_t v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> sh) & 0xFFFFu);
+        *reinterpret_cast<uint4*>(pcol + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<uint4*>(pcol + 64 + ty * 4) = make_uint4(v[4], v[5], v[6], v[7]);
+    }
+}
+
+// Pivot k = kb + U of the closure: relax with the snapshot in buffer U & 1,
+// publish pivot k + 1 into the other buffer, one barrier.
+template <int U>
+__device__ __forceinline__ void q_close_step(uint32_t (&c)[8][4], uint32_t* prow, uint32_t* pcol, int k, int kr,
+                                             int tx, int ty) {
+    constexpr int buf = U & 1;
+    const uint4 al = *reinterpret_cast<const uint4*>(pcol + buf * kTile + ty * 4);
+    const uint4 ah = *reinterpret_cast<const uint4*>(pcol + buf * kTile + 64 + ty * 4);
+    const uint4 bq = *reinterpret_cast<const uint4*>(prow + buf * kQTileW + tx * 4);
+    const uint32_t a[8] = {al.x, al.y, al.z, al.w, ah.x, ah.y, ah.z, ah.w};
+    const uint32_t b[4] = {bq.x, bq.y, bq.z, bq.w};
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) c[r][w] = __viaddmin_u16x2(a[r], b[w], c[r][w]);
+    if (k + 1 < kr) q_publish<(U + 1) & 7>(c, k + 1, prow + (buf ^ 1) * kQTileW, pcol + (buf ^ 1) * kTile, tx, ty);
+    __syncthreads();
+}
+
+// Closure of the diagonal block held as c (rows own_row(ty, r), words
+// tx*4..) over its first `kv` pivots, rounded up to a multiple of 8 (the
+// pivots past kv lie outside the graph: CAP rows and columns, which change
+// nothing). prow: 2 x 64 words, pcol: 2 x 128 duplicated words, snapshots of
+// the pivot row and column double-buffered so that each pivot costs one
+// barrier and no thread reads what another writes in the same step.
+__device__ __forceinline__ void q_close(uint32_t (&c)[8][4], uint32_t* prow, uint32_t* pcol, int kv, int tx, int ty) {
+    const int kr = (kv + 7) & ~7;
+    q_publish<0>(c, 0, prow, pcol, tx, ty);
+    __syncthreads();
+    for (int kb = 0; kb < kr; kb += 8) {
+        q_close_step<0>(c, prow, pcol, kb + 0, kr, tx, ty);
+        q_close_step<1>(c, prow, pcol, kb + 1, kr, tx, ty);
+        q_close_step<2>(c, prow, pcol, kb + 2, kr, tx, ty);
+        q_close_step<3>(c, prow, pcol, kb + 3, kr, tx, ty);
+        q_close_step<4>(c, prow, pcol, kb + 4, kr, tx, ty);
+        q_close_step<5>(c, prow, pcol, kb + 5, kr, tx, ty);
+        q_close_step<6>(c, prow, pcol, kb + 6, kr, tx, ty);
+        q_close_step<7>(c, prow, pcol, kb + 7, kr, tx, ty);
+    }
+}
+
+// Per-graph proof state, in shared memory.
+struct QProof {
+    unsigned bad;   // some entry is neither INF nor in [0, CAP)
+    unsigned wmax;  // largest finite entry
+    unsigned rmax;  // largest result below CAP
+};
+
+// W = encode(G) for an n x n int32 graph at G (row-major, rows need not be
+// aligned); W has `ld` values (ld / 2 words) per row and ld rows, padding CAP.
+__device__ __forceinline__ void q_encode(const int* __restrict__ G, int n, uint32_t* Wm, int ld, QProof* pf, int tid) {
+    unsigned bad = 0, wmax = 0;
+    const int vecs = ld / 8;  // 8 values (4 words) per step
+    for (int q = tid; q < ld * vecs; q += kThreads) {
+        const int i = q / vecs, j0 = (q % vecs) * 8;
+        uint32_t e[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int j = j0 + u;
+            uint32_t x = kQCap;
+            if (i < n && j < n) {
+                const int v = G[(int64_t)i * n + j];
+                if (v != kInf) {
+                    if (v >= 0 && (uint32_t)v < kQCap) {
+                        x = (uint32_t)v;
+                        wmax = max(wmax, x);
+                    } else {
+                        bad = 1;
+                    }
+                }
+            }
+            e[u] = x;
+        }
+        *reinterpret_cast<uint4*>(Wm + (int64_t)i * (ld / 2) + j0 / 2) =
+            make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+    }
+    if (bad) atomicOr(&pf->bad, 1u);
+    if (wmax) atomicMax(&pf->wmax, wmax);
+}
+
+// Largest result below CAP over the graph's n x n entries.
+__device__ __forceinline__ void q_rmax(const uint32_t* Wm, int n, int ld, QProof* pf, int tid) {
+    unsigned m = 0;
+    const int words = (n + 1) / 2;
+    for (int q = tid; q < n * words; q += kThreads) {
+        const int i = q / words, w = q % words;
+        const uint32_t x = Wm[(int64_t)i * (ld / 2) + w];
+        const uint32_t lo = x & 0xFFFFu, hi = x >> 16;
+        if (lo < kQCap) m = max(m, lo);
+        if (2 * w + 1 < n && hi < kQCap) m = max(m, hi);
+    }
+    if (m) atomicMax(&pf->rmax, m);
+}
+
+// G = decode(W) (CAP -> INF) for the graph's n x n entries.
+__device__ __forceinline__ void q_decode(const uint32_t* Wm, int* __restrict__ G, int n, int ld, int tid) {
+    for (int q = tid; q < n * n; q += kThreads) {
+        const int i = q / n, j = q % n;
+        const uint32_t x = (Wm[(int64_t)i * (ld / 2) + (j >> 1)] >> ((j & 1) * 16)) & 0xFFFFu;
+        G[q] = (x == kQCap) ? kInf : (int)x;
+    }
+}
+
+// The blocked sweep of W (ld x ld values, T = ld / 128 blocks, n valid).
+// colD: 128 x ld duplicated words; rowP: 128 x ld / 2 words.
+__device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* colD, uint32_t* rowP, uint32_t* smem,
+                                        int one) {
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int T = ld / kTile;
+    const int64_t ldw = ld / 2;
+    for (int pt = 0; pt < T; ++pt) {
+        const int p0 = pt * kTile, pw0 = p0 / 2;
+        const int kv = min(kTile, n - p0);
+        const int nslab = (kv + kSlab - 1) / kSlab;
+        {  // 1. diagonal block: closure in registers, then W, rowP[k][P] and colD[k][P]
+            uint32_t c[8][4];
+            q_load_tile(c, Wm, ldw, p0, pw0, tx, ty);
+            q_close(c, smem, smem + 2 * kQTileW, kv, tx, ty);
+            q_store_tile(c, Wm, ldw, p0, pw0, tx, ty);
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                *reinterpret_cast<uint4*>(rowP + (int64_t)own_row(ty, r) * ldw + pw0 + tx * 4) =
+                    make_uint4(c[r][0], c[r][1], c[r][2], c[r][3]);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int k = 2 * (tx * 4 + w) + h;
+                    uint32_t v[8];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> (16 * h)) & 0xFFFFu);
+                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + p0 + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
+                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + p0 + 64 + ty * 4) =
+                        make_uint4(v[4], v[5], v[6], v[7]);
+                }
+            }
+            __threadfence_block();
+            __syncthreads();
+        }
+        uint32_t c[8][4];
+        // 2. row panel: W[P][J] = min(W[P][J], Dg* (x) W[P][J]); rowP[k][J] = result rows
+        for (int tj = 0; tj < T; ++tj) {
+            if (tj == pt) continue;
+            const int64_t w0 = (int64_t)tj * kQTileW;
+            q_load_tile(c, Wm, ldw, p0, w0, tx, ty);
+            q_mainloop(
+                c, nslab, smem,
+                [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, p0, tid); },
+                [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, Wm, ldw, p0 + s * kSlab, w0, tid); },
+                tx, ty, one);
+            __syncthreads();  // every thread read its B rows (rows of this tile) before any is rewritten
+            q_store_tile(c, Wm, ldw, p0, w0, tx, ty);
+            q_store_tile(c, rowP, ldw, 0, w0, tx, ty);
+        }
+        // 3. column panel: W[I][P] = min(W[I][P], W[I][P] (x) Dg*); colD[k][I] = result columns
+        for (int ti = 0; ti < T; ++ti) {
+            if (ti == pt) continue;
+            const int64_t r0 = (int64_t)ti * kTile;
+            q_load_tile(c, Wm, ldw, r0, pw0, tx, ty);
+            q_mainloop(
+                c, nslab, smem,
+                [&](uint32_t* dst, int s) { q_load_transposed_dup(dst, Wm, ldw, r0, pw0 + s * (kSlab / 2), tid); },
+                [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, pw0, tid); },
+                tx, ty, one);
+            __syncthreads();  // every thread read its A columns (of this tile) before any is rewritten
+            q_store_tile(c, Wm, ldw, r0, pw0, tx, ty);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int k = 2 * (tx * 4 + w) + h;
+                    uint32_t v[8];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> (16 * h)) & 0xFFFFu);
+                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + r0 + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
+                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + r0 + 64 + ty * 4) =
+                        make_uint4(v[4], v[5], v[6], v[7]);
+                }
+            }
+        }
+        __threadfence_block();
+        __syncthreads();  // panels complete before the remainder reads them
+        // 4. remainder: W[I][J] = min(W[I][J], colD[:, I]^T (x) rowP[:, J])
+        for (int ti = 0; ti < T; ++ti) {
+            if (ti == pt) continue;
+            const int64_t r0 = (int64_t)ti * kTile;
+            for (int tj = 0; tj < T; ++tj) {
+                if (tj == pt) continue;
+                const int64_t w0 = (int64_t)tj * kQTileW;
+                q_load_tile(c, Wm, ldw, r0, w0, tx, ty);
+                q_mainloop(
+                    c, nslab, smem,
+                    [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, r0, tid); },
+                    [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, w0, tid); },
+                    tx, ty, one);
+                q_store_tile(c, Wm, ldw, r0, w0, tx, ty);
+                __syncthreads();  // the next tile's prologue refills the ring
+            }
+        }
+        __threadfence_block();
+        __syncthreads();
+    }
+}
+
+}  // namespace fw

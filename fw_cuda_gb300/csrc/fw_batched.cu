@@ -33,6 +33,7 @@
 #include <string>
 #include <vector>
 
+#include "fw_batch_p16.cuh"
 #include "fw_common.cuh"
 #include "fw_internal.h"
 #include "fw_tile.cuh"
@@ -42,6 +43,10 @@ namespace {
 
 constexpr int kBuckets = 5;
 constexpr int kBatchMaxN = 4096;
+// Device counters of one launch: one per bucket of the int32 kernel, the
+// packed kernel's graph counter, the length of its hand-back list.
+constexpr int kCounters = kBuckets + 2;
+constexpr int kQCounter = kBuckets, kFallbackCount = kBuckets + 1;
 // Form-A columns of the per-CTA sweep (see kColsA), chosen apart from the
 // TMA-fed remainder's because its slabs arrive by cp.async.
 constexpr unsigned kBatchedColsA = cols_below(5);
@@ -234,21 +239,73 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int6
     }
 }
 
+// Large graphs in the exact packed 16-bit form (fw_batch_p16.cuh): one CTA
+// per graph, persistent over items [start, start + count) (all with
+// 128 < n <= kQMaxN). A graph that does not qualify, or whose result the
+// proof cannot take, is left untouched and its item index appended to
+// `fallback` for the int32 kernel, which runs after this one.
+__global__ void __launch_bounds__(kThreads, 2)
+    fw_batched_p16_kernel(int* __restrict__ packed, const BatchItem* __restrict__ items, int start, int count,
+                          int* __restrict__ counters, int* __restrict__ fallback, uint32_t* __restrict__ ws,
+                          int64_t ws_words, int one) {
+    extern __shared__ __align__(128) uint32_t qsm[];
+    __shared__ int s_item;
+    __shared__ QProof pf;
+    uint32_t* Wm = ws + (int64_t)blockIdx.x * ws_words;
+    const int tid = threadIdx.x;
+    for (;;) {
+        __syncthreads();  // the previous graph's readers of s_item and pf are done
+        if (tid == 0) {
+            s_item = atomicAdd(&counters[kQCounter], 1);
+            pf.bad = 0;
+            pf.wmax = 0;
+            pf.rmax = 0;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= count) break;
+        const BatchItem item = items[start + it];
+        const int n = item.n;
+        const int ld = (n + kTile - 1) / kTile * kTile;
+        uint32_t* colD = Wm + (int64_t)ld * (ld / 2);
+        uint32_t* rowP = colD + (int64_t)kTile * ld;
+        int* G = packed + item.offset;
+        q_encode(G, n, Wm, ld, &pf, tid);
+        __syncthreads();
+        bool take = pf.bad == 0;
+        if (take) {
+            q_sweep(Wm, n, ld, colD, rowP, qsm, one);
+            q_rmax(Wm, n, ld, &pf, tid);
+            __syncthreads();
+            take = pf.rmax + pf.wmax < kQCap;
+        }
+        if (take) {
+            q_decode(Wm, G, n, ld, tid);
+        } else if (tid == 0) {
+            fallback[atomicAdd(&counters[kFallbackCount], 1)] = start + it;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 2)
     fw_batched_kernel(int* __restrict__ packed, const BatchItem* __restrict__ items, BatchSched sched,
-                      int* __restrict__ counters, int* __restrict__ ws, int64_t ldw, int one) {
+                      int* __restrict__ counters, const int* __restrict__ fallback, int* __restrict__ ws, int64_t ldw,
+                      int one) {
     extern __shared__ __align__(128) int smem[];
     __shared__ int s_item[8];
-    // bucket 0: whole CTA per graph, solved in place
+    // bucket 0: whole CTA per graph, solved in place: first the graphs the
+    // packed kernel (which ran before this one) handed back, then the large
+    // graphs it does not take
     int* colT = ws + (int64_t)blockIdx.x * 2 * kTile * ldw;
     int* rowP = colT + (int64_t)kTile * ldw;
+    const int handed_back = counters[kFallbackCount];
     for (;;) {
         if (threadIdx.x == 0) s_item[0] = atomicAdd(&counters[0], 1);
         __syncthreads();
         const int it = s_item[0];
         __syncthreads();
-        if (it >= sched.count[0]) break;
-        const BatchItem item = items[sched.start[0] + it];
+        if (it >= handed_back + sched.count[0]) break;
+        const BatchItem item = it < handed_back ? items[fallback[it]] : items[sched.start[0] + it - handed_back];
         blocked_in_cta<false>(packed + item.offset, item.n, item.n, colT, rowP, ldw, smem, one);
     }
     small_bucket<128, 1>(packed, items, sched.start[1], sched.count[1], &counters[1], smem, s_item);
@@ -287,6 +344,14 @@ struct fw_batch_plan {
     int* d_counters = nullptr;
     int* d_ws = nullptr;
     int ws_ctas = 0;
+    // Graphs with n > 128: items [big_start, big_start + big_count), the
+    // first big_int32 of them (n > kQMaxN) always on the int32 path.
+    int big_start = 0, big_count = 0, big_int32 = 0;
+    bool use_p16 = false;      // the rest by the packed kernel (else all on the int32 path)
+    int q_blocks_per_sm = 2;
+    int64_t q_ws_words = 0;    // packed workspace words per CTA
+    uint32_t* d_qws = nullptr;
+    int* d_fallback = nullptr;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t exec = nullptr;
     const int32_t* exec_packed = nullptr;
@@ -295,14 +360,23 @@ struct fw_batch_plan {
 
 namespace {
 
+// Splits the n > 128 graphs between the packed and the int32 kernels.
+void apply_form(fw_batch_plan* p) {
+    const int q = p->big_count - p->big_int32;
+    p->sched.start[0] = p->big_start;
+    p->sched.count[0] = (p->use_p16 && q > 0) ? p->big_int32 : p->big_count;
+}
+
+int packed_count(const fw_batch_plan* p) { return p->use_p16 ? p->big_count - p->big_int32 : 0; }
+
 void plan_describe(fw_batch_plan* p) {
-    char buf[256];
+    char buf[320];
     std::snprintf(buf, sizeof(buf),
-                  "graphs=%lld maxn=%d buckets[n>128:%d n<=128:%d n<=64:%d/g%d n<=32:%d/g%d n<=16:%d/g%d] "
-                  "ctas/sm=%d",
-                  (long long)p->count, p->maxn, p->sched.count[0], p->sched.count[1], p->sched.count[2],
-                  p->sched.groups[2], p->sched.count[3], p->sched.groups[3], p->sched.count[4], p->sched.groups[4],
-                  p->blocks_per_sm);
+                  "graphs=%lld maxn=%d buckets[n>128:%d (packed %d, int32 %d) n<=128:%d n<=64:%d/g%d n<=32:%d/g%d "
+                  "n<=16:%d/g%d] ctas/sm=%d packed ctas/sm=%d",
+                  (long long)p->count, p->maxn, p->big_count, packed_count(p), p->sched.count[0], p->sched.count[1],
+                  p->sched.count[2], p->sched.groups[2], p->sched.count[3], p->sched.groups[3], p->sched.count[4],
+                  p->sched.groups[4], p->blocks_per_sm, p->q_blocks_per_sm);
     p->schedule = buf;
 }
 
@@ -313,10 +387,17 @@ void drop_graph(fw_batch_plan* p) {
 }
 
 int launch_direct(fw_batch_plan* p, int32_t* d_packed, cudaStream_t s) {
-    FW_CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, kBuckets * sizeof(int), s));
+    FW_CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, kCounters * sizeof(int), s));
+    const int q = packed_count(p);
+    if (q > 0) {
+        fw_batched_p16_kernel<<<p->sms * p->q_blocks_per_sm, kThreads, kQSmemBytes, s>>>(
+            d_packed, p->d_items, p->big_start + p->big_int32, q, p->d_counters, p->d_fallback, p->d_qws,
+            p->q_ws_words, 1);
+        FW_LAUNCH_CHECK("fw_batched_p16_kernel");
+    }
     const int grid = p->sms * p->blocks_per_sm;
-    fw_batched_kernel<<<grid, kThreads, kSmemBytes, s>>>(d_packed, p->d_items, p->sched, p->d_counters, p->d_ws,
-                                                         p->ldw, 1);
+    fw_batched_kernel<<<grid, kThreads, kSmemBytes, s>>>(d_packed, p->d_items, p->sched, p->d_counters,
+                                                         p->d_fallback, p->d_ws, p->ldw, 1);
     FW_LAUNCH_CHECK("fw_batched_kernel");
     return FW_OK;
 }
@@ -378,11 +459,18 @@ int fw_batch_plan_create(fw_batch_plan** out, const int32_t* h_sizes, const int6
         p->sched.count[b] = 0;
         p->sched.groups[b] = 1;
     }
+    int32_t maxq = 0;  // largest graph the packed path takes
     for (int64_t q = 0; q < count; ++q) {
         const int b = bucket_of(items[q].n);
         if (p->sched.count[b] == 0) p->sched.start[b] = (int)q;
         p->sched.count[b]++;
+        if (b == 0 && items[q].n > kQMaxN) p->big_int32++;
+        if (b == 0 && items[q].n <= kQMaxN) maxq = std::max(maxq, items[q].n);
     }
+    p->big_start = p->sched.start[0];
+    p->big_count = p->sched.count[0];
+    p->use_p16 = p->big_count > p->big_int32;
+    apply_form(p);
     // Defaults before tuning: pack small graphs 4 (n <= 64) or 8 (n <= 32) per CTA.
     p->sched.groups[2] = 4;
     p->sched.groups[3] = 8;
@@ -401,8 +489,22 @@ int fw_batch_plan_create(fw_batch_plan** out, const int32_t* h_sizes, const int6
             rc = cuda_error(cudaGetLastError(), "cudaFuncSetAttribute");
             break;
         }
+        if (p->big_count > p->big_int32) {
+            if (cudaFuncSetAttribute(fw_batched_p16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kQSmemBytes) != cudaSuccess) {
+                rc = cuda_error(cudaGetLastError(), "cudaFuncSetAttribute");
+                break;
+            }
+            p->q_ws_words = q_ws_words(((int64_t)maxq + kTile - 1) / kTile * kTile);
+            if (cudaMalloc(&p->d_qws, sizeof(uint32_t) * (size_t)p->q_ws_words * p->sms * 2) != cudaSuccess ||
+                cudaMalloc(&p->d_fallback, sizeof(int) * (size_t)p->big_count) != cudaSuccess) {
+                cudaGetLastError();
+                rc = set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_create: device allocation failed");
+                break;
+            }
+        }
         if (cudaMalloc(&p->d_items, sizeof(BatchItem) * count) != cudaSuccess ||
-            cudaMalloc(&p->d_counters, sizeof(int) * kBuckets) != cudaSuccess ||
+            cudaMalloc(&p->d_counters, sizeof(int) * kCounters) != cudaSuccess ||
             cudaMalloc(&p->d_ws, sizeof(int) * (size_t)2 * kTile * p->ldw * p->ws_ctas) != cudaSuccess) {
             cudaGetLastError();
             rc = set_error(FW_ERR_NO_MEMORY, "fw_batch_plan_create: device allocation failed");
@@ -434,6 +536,8 @@ void fw_batch_plan_destroy(fw_batch_plan* p) {
     cudaFree(p->d_items);
     cudaFree(p->d_counters);
     cudaFree(p->d_ws);
+    cudaFree(p->d_qws);
+    cudaFree(p->d_fallback);
     delete p;
 }
 
@@ -479,8 +583,10 @@ int fw_apsp_batched_i32(fw_batch_plan* p, int32_t* d_packed, fw_stream_t stream)
 }
 
 // Times the candidate schedules on a scratch copy of the batch and keeps the
-// fastest: per small bucket the number of graphs per CTA, then the number of
-// resident CTAs per SM for the whole batch. Synchronises the stream.
+// fastest: the arithmetic form of the graphs with n > 128 (exact packed
+// 16-bit with its CTAs per SM, or int32), per small bucket the number of
+// graphs per CTA, then the number of resident CTAs per SM of the int32 kernel
+// for the whole batch. Synchronises the stream.
 int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_t stream) {
     if (!p || !d_packed) return set_error(FW_ERR_INVALID_ARGUMENT, "fw_batch_plan_autotune: NULL argument");
     int dev = 0;
@@ -499,7 +605,7 @@ int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const BatchSched full = p->sched;
+    const BatchSched full = p->sched;  // groups of the small buckets and their counts
     auto time_once = [&](float* ms) -> int {
         FW_CUDA_TRY(cudaMemcpyAsync(scratch, d_packed, bytes, cudaMemcpyDeviceToDevice, s));
         FW_CUDA_TRY(cudaEventRecord(e0, s));
@@ -520,11 +626,43 @@ int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_
         return FW_OK;
     };
     int rc = FW_OK;
+    auto set_counts = [&](bool big, bool small) {
+        for (int q = 1; q < kBuckets; ++q) p->sched.count[q] = small ? full.count[q] : 0;
+        apply_form(p);
+        if (!big) {
+            p->sched.count[0] = 0;
+            p->use_p16 = false;
+        }
+    };
+    // 1. Graphs with n > 128 alone: the packed kernel (1 or 2 CTAs per SM,
+    //    int32 for the graphs it hands back or cannot take) against the int32
+    //    kernel for all of them.
+    if (p->big_count > p->big_int32) {
+        float best = 1e30f;
+        bool form = true;
+        int qbps = p->q_blocks_per_sm;
+        for (int trial = 0; trial < 3 && rc == FW_OK; ++trial) {
+            p->use_p16 = trial < 2;
+            p->q_blocks_per_sm = trial == 1 ? 1 : 2;
+            set_counts(true, false);
+            float ms = 0;
+            rc = best_of(&ms);
+            if (rc == FW_OK && ms < best) {
+                best = ms;
+                form = p->use_p16;
+                qbps = p->q_blocks_per_sm;
+            }
+        }
+        p->use_p16 = form;
+        p->q_blocks_per_sm = qbps;
+    }
+    const bool form = p->use_p16;
+    // 2. Each small bucket alone: graphs per CTA.
     const int options[kBuckets][3] = {{1, 1, 1}, {1, 1, 1}, {1, 4, 4}, {1, 4, 8}, {1, 4, 8}};
     for (int b = 2; b < kBuckets && rc == FW_OK; ++b) {
         if (full.count[b] == 0) continue;
-        // only bucket b runs
-        for (int q = 0; q < kBuckets; ++q) p->sched.count[q] = (q == b) ? full.count[q] : 0;
+        set_counts(false, false);
+        p->sched.count[b] = full.count[b];
         float best = 1e30f;
         int choice = full.groups[b];
         for (int o = 0; o < 3 && rc == FW_OK; ++o) {
@@ -539,7 +677,9 @@ int fw_batch_plan_autotune(fw_batch_plan* p, const int32_t* d_packed, fw_stream_
         }
         p->sched.groups[b] = choice;
     }
-    for (int q = 0; q < kBuckets; ++q) p->sched.count[q] = full.count[q];
+    p->use_p16 = form;
+    set_counts(true, true);
+    // 3. The whole batch: resident CTAs per SM of the int32 kernel.
     if (rc == FW_OK) {
         float best = 1e30f;
         int choice = p->blocks_per_sm;

@@ -136,3 +136,46 @@ def test_batched_workload_parameters():
     assert 80 <= np.median(sizes) <= 100
     s2, d2, e2 = workloads.batched_params()
     assert np.array_equal(sizes, s2) and np.array_equal(seeds, e2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("autotune", [False, True])
+def test_packed_large_graphs_and_their_fallbacks(fw, cuda, oracle, autotune):
+    """Graphs with 128 < n <= 1024 take the exact packed 16-bit path unless an
+    entry is outside [0, 32767) u {INF} (a negative or a too large weight) or
+    a distance comes too close to the 16-bit cap for the proof (a long chain
+    of heavy edges); those graphs, and graphs with n > 1024, are solved by the
+    int32 path. Every graph against the oracle."""
+    rng = np.random.default_rng(11)
+    graphs = []
+    graphs.append(oracle.generate_graph(200, 0.6, 1, 1, 100))          # packed
+    W = oracle.generate_graph(300, 0.3, 2, 1, 100).astype(np.int64)    # a negative edge, no negative cycle
+    p = rng.integers(0, 60, 300)
+    W = np.where(W < INF, W + p[:, None] - p[None, :], INF)
+    np.fill_diagonal(W, 0)
+    graphs.append(W.astype(np.int32))
+    W = oracle.generate_graph(257, 0.5, 3, 1, 100)                      # one weight >= 32767
+    W[5, 7] = 40000
+    graphs.append(W)
+    chain = np.full((400, 400), INF, dtype=np.int32)                    # distances past the cap
+    np.fill_diagonal(chain, 0)
+    chain[np.arange(399), np.arange(1, 400)] = 1000
+    graphs.append(chain)
+    graphs.append(oracle.generate_graph(129, 0.9, 4, 1, 100))          # packed
+    graphs.append(oracle.generate_graph(1024, 0.3, 5, 1, 100))         # packed, the largest it takes
+    graphs.append(oracle.generate_graph(1025, 0.3, 6, 1, 100))         # int32 (n > 1024)
+    graphs.append(oracle.generate_graph(700, 0.05, 7, 0, 25000))       # either, by the proof
+    sizes = np.array([g.shape[0] for g in graphs], dtype=np.int32)
+    offsets, total = fw.pack_offsets(sizes)
+    packed = np.full(total, -7, dtype=np.int32)
+    for g, W in enumerate(graphs):
+        packed[offsets[g]: offsets[g] + W.size] = W.ravel()
+    plan, d = _solve_all(fw, cuda, sizes, offsets, packed, autotune)
+    out = d.cpu().numpy()
+    _check_all(oracle, sizes, offsets, packed, out)
+    assert "n>128:8" in plan.describe()
+    for rep in range(2):  # replays on fresh copies (the hand-back list is rebuilt every launch)
+        d.copy_(cuda.from_numpy(packed))
+        plan.solve(d)
+        cuda.cuda.synchronize()
+        assert np.array_equal(d.cpu().numpy(), out)

@@ -122,9 +122,13 @@ def test_batch_equals_single_graphs(cuda):
 
 
 def test_gradient_matches_central_differences_n96(cuda, oracle):
-    """The same check on a larger graph (n = 96): 400 sampled edges, every
-    edge with a nonzero gradient among them weighted in, central differences
-    in FP64 through the oracle sweep, 1e-3 relative."""
+    """The same check on a larger graph (n = 96), 400 sampled edges (300 on
+    shortest paths), central differences in FP64 through the oracle sweep,
+    1e-3 relative. With this many paths some pairs have an alternative path
+    within eps of the shortest: the loss then has a kink inside [w - eps,
+    w + eps] and no difference quotient is its derivative. Such edges are
+    recognised by their one-sided differences disagreeing and left out (at
+    most 5 % of the sample); every other edge must match."""
     from fw_cuda_gb300 import autograd as A
 
     rng = np.random.default_rng(96)
@@ -148,12 +152,20 @@ def test_gradient_matches_central_differences_n96(cuda, oracle):
     assert len(on_paths) > 200
     pick = [on_paths[i] for i in rng.choice(len(on_paths), 300, replace=False)]
     pick += [off_paths[i] for i in rng.choice(len(off_paths), 100, replace=False)]
+    l0 = loss(W64)
+    kinks = 0
     for u, v in pick:
         Wp, Wm = W64.copy(), W64.copy()
         Wp[u, v] += eps
         Wm[u, v] -= eps
-        fd = (loss(Wp) - loss(Wm)) / (2 * eps)
+        lp, lm = loss(Wp), loss(Wm)
+        fwd, bwd = (lp - l0) / eps, (l0 - lm) / eps
+        if abs(fwd - bwd) > 1e-6 * max(1.0, abs(fwd)):
+            kinks += 1  # a shortest path changes inside the window
+            continue
+        fd = (lp - lm) / (2 * eps)
         assert abs(fd - grad[u, v]) <= 1e-3 * max(1.0, abs(fd)), (u, v, fd, grad[u, v])
+    assert kinks <= 0.05 * len(pick), kinks
 
 
 def test_batch_workload_against_fp64_sweep(cuda, oracle):
