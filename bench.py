@@ -18,7 +18,8 @@ matrix back. `auto_path` is the same workload through FW_VARIANT_AUTO (the
 exact packed 16-bit fast path, taken only when provably identical), with its
 own roofline and e2e; `verified` compares its result with the int32 result
 bit for bit and checks sampled full rows of the int32 result against the
-oracle's Dijkstra. With --gpus N (torchrun) every rank solves its own copy of
+oracle's Dijkstra, and 64 graphs of the batched result against the oracle's
+sweep. With --gpus N (torchrun) every rank solves its own copy of
 the workload (replicas; the path has no data-parallel exchange) and `value`
 is the sum over ranks, timed by the slowest rank.
 
@@ -421,9 +422,9 @@ def run_ours(args) -> None:
         auto = run_auto(args, F, torch, stream, work, pristine, h_in, n, world, local, relax, head_out, hbm_peak,
                         hbm_measured)
 
-    batched = None
+    batched, batched_data = None, None
     if not args.no_batched:
-        batched = run_batched(args, F, torch, stream, world)
+        batched, batched_data = run_batched(args, F, torch, stream, world)
 
     diff = None
     if not args.no_diff:
@@ -449,6 +450,8 @@ def run_ours(args) -> None:
         srcs = sorted({0, n - 1, *[int(x) for x in rng.choice(n, size=min(n, 6), replace=False)]})
         rows = {s: head_out[s].cpu().numpy() for s in srcs}
         verified.update(dijkstra_rows(h_in.numpy(), rows, os.cpu_count() or 1))
+        if batched_data is not None:
+            verified.update(batched_sample_check(batched_data, 64, os.cpu_count() or 1))
 
     launches = sum(v["launches"] for v in prof.values())
     if rank == 0:
@@ -616,14 +619,41 @@ def run_batched(args, F, torch, stream, world) -> dict:
             F.apsp_i32(base + 4 * int(offsets[g]), int(sizes[g]), 32, args.kappa, 2, stream)
 
     t_batched = timed(lambda: plan.solve(work, stream), args.steps)
+    result = work.cpu().numpy()  # the last timed solve's output, for the sampled check
     t_loop = timed(loop, max(1, min(args.steps, 2)))
     plan.close()
     count = len(sizes)
-    return {"workload": "4096 graphs, n log-uniform [16, 512], density U(0.05, 1), weights U[1, 100], seed 1234",
-            "graphs_per_s": world * count / t_batched, "relax_per_s": world * relax / t_batched,
-            "ms_per_step": 1e3 * t_batched, "schedule": schedule,
-            "loop_plain_graphs_per_s": world * count / t_loop, "loop_plain_ms_per_step": 1e3 * t_loop,
-            "speedup_vs_loop": t_loop / t_batched, "relaxations_per_step": relax}
+    rec = {"workload": "4096 graphs, n log-uniform [16, 512], density U(0.05, 1), weights U[1, 100], seed 1234",
+           "graphs_per_s": world * count / t_batched, "relax_per_s": world * relax / t_batched,
+           "ms_per_step": 1e3 * t_batched, "schedule": schedule,
+           "loop_plain_graphs_per_s": world * count / t_loop, "loop_plain_ms_per_step": 1e3 * t_loop,
+           "speedup_vs_loop": t_loop / t_batched, "relaxations_per_step": relax}
+    return rec, (sizes, offsets, packed, result)
+
+
+def batched_sample_check(data, count: int, threads: int) -> dict:
+    """The 8 largest graphs and `count - 8` seeded random others of the
+    batched result against the oracle's sweep of each graph (parallel host
+    threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    sizes, offsets, packed, out = data
+    rng = np.random.default_rng(4096)
+    largest = np.argsort(-sizes, kind="stable")[:8]
+    rest = np.setdiff1d(np.arange(len(sizes)), largest)
+    pick = sorted(largest.tolist() + rng.choice(rest, min(len(rest), count - 8), replace=False).tolist())
+
+    def ok(g):
+        n, o = int(sizes[g]), int(offsets[g])
+        return np.array_equal(out[o:o + n * n], O.fw_i32(packed[o:o + n * n].reshape(n, n)).ravel())
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        good = sum(ex.map(ok, pick))
+    return {"batched_graphs_vs_oracle": f"{good}/{len(pick)}", "batched_all_match": good == len(pick),
+            "batched_check_seconds": round(time.perf_counter() - t0, 2)}
 
 
 def run_diff(args, torch, stream, world) -> dict:

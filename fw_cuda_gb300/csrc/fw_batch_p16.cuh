@@ -43,8 +43,10 @@ constexpr int kQSlabA = kSlab * kTile;                // words: 32 pivots x 128 
 constexpr int kQSlabB = kSlab * kQTileW;              // words: 32 pivots x 64 words
 constexpr int kQStageWords = kQSlabA + kQSlabB;
 constexpr int kQSmemBytes = kStages * kQStageWords * 4;  // 72 KB
-// Words (bit w of the thread's 4) that take form A.
-constexpr unsigned kQWordsA = 0x5u;
+// Words (bit w of the thread's 4) that take form A: {1, 2} (the batched
+// workload in 3.67 ms; {0, 2} 3.72, {0, 1} 3.71, {1, 3} 3.70, {0, 3} 3.74,
+// {0} 3.78, {1, 2, 3} 3.72 ms).
+constexpr unsigned kQWordsA = 0x6u;
 
 // Workspace words of one CTA for graphs up to `ld` values wide (ld a
 // multiple of 128): W, colD (128 x ld), rowP (128 x ld / 2).
@@ -63,6 +65,9 @@ __device__ __forceinline__ uint32_t q_relax2(bool form_a, uint32_t acc, uint32_t
 
 // acc = min(acc, A (x) B) over one 32-pivot slab in shared memory: A k-major
 // [32][128] duplicated words (rows of the tile), B k-major [32][64] words.
+// NR = 8: all of the thread's rows; NR = 4: its first four (rows 64.. of the
+// tile lie outside the graph).
+template <int NR>
 __device__ __forceinline__ void q_relax_slab(uint32_t (&c)[8][4], const uint32_t* As, const uint32_t* Bs, int tx,
                                              int ty, int one) {
 #pragma unroll 1
@@ -70,24 +75,35 @@ __device__ __forceinline__ void q_relax_slab(uint32_t (&c)[8][4], const uint32_t
         uint32_t a0[8], a1[8], b0[4], b1[4];
         {
             const uint4 l0 = *reinterpret_cast<const uint4*>(As + kk * kTile + ty * 4);
-            const uint4 h0 = *reinterpret_cast<const uint4*>(As + kk * kTile + 64 + ty * 4);
             const uint4 l1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + ty * 4);
-            const uint4 h1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + 64 + ty * 4);
             const uint4 q0 = *reinterpret_cast<const uint4*>(Bs + kk * kQTileW + tx * 4);
             const uint4 q1 = *reinterpret_cast<const uint4*>(Bs + (kk + 1) * kQTileW + tx * 4);
             a0[0] = l0.x; a0[1] = l0.y; a0[2] = l0.z; a0[3] = l0.w;
-            a0[4] = h0.x; a0[5] = h0.y; a0[6] = h0.z; a0[7] = h0.w;
             a1[0] = l1.x; a1[1] = l1.y; a1[2] = l1.z; a1[3] = l1.w;
-            a1[4] = h1.x; a1[5] = h1.y; a1[6] = h1.z; a1[7] = h1.w;
+            if (NR == 8) {
+                const uint4 h0 = *reinterpret_cast<const uint4*>(As + kk * kTile + 64 + ty * 4);
+                const uint4 h1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + 64 + ty * 4);
+                a0[4] = h0.x; a0[5] = h0.y; a0[6] = h0.z; a0[7] = h0.w;
+                a1[4] = h1.x; a1[5] = h1.y; a1[6] = h1.z; a1[7] = h1.w;
+            }
             b0[0] = q0.x; b0[1] = q0.y; b0[2] = q0.z; b0[3] = q0.w;
             b1[0] = q1.x; b1[1] = q1.y; b1[2] = q1.z; b1[3] = q1.w;
         }
 #pragma unroll
-        for (int r = 0; r < 8; ++r)
+        for (int r = 0; r < NR; ++r)
 #pragma unroll
             for (int w = 0; w < 4; ++w)
                 c[r][w] = q_relax2(((kQWordsA >> w) & 1u) != 0, c[r][w], a0[r], b0[w], a1[r], b1[w], one);
     }
+}
+
+// Which of its rows a warp updates in a tile with `rows` rows inside the
+// graph: warp w holds rows 8w .. 8w + 7 and 64 + 8w .. 64 + 8w + 7; rows
+// outside the graph stay CAP whatever the pivots, so a warp skips them
+// (2: all eight, 1: the first four, 0: none).
+__device__ __forceinline__ int q_row_mode(int rows) {
+    const int w = threadIdx.x >> 5;
+    return (64 + 8 * w < rows) ? 2 : (8 * w < rows ? 1 : 0);
 }
 
 // The thread's 8 rows x 4 words of the tile at (r0, word w0) of a packed
@@ -141,10 +157,12 @@ __device__ __forceinline__ void q_load_transposed_dup(uint32_t* dst, const uint3
 }
 
 // Three-stage cp.async pipeline over `nslab` slabs (the int32 mainloop's
-// schedule); la / lb fill slab s of A / B.
+// schedule); la / lb fill slab s of A / B. `rows`: the tile's rows inside the
+// graph (see q_row_mode).
 template <class LA, class LB>
-__device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, uint32_t* smem, LA la, LB lb, int tx,
-                                           int ty, int one) {
+__device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, int rows, uint32_t* smem, LA la, LB lb,
+                                           int tx, int ty, int one) {
+    const int mode = q_row_mode(rows);
 #pragma unroll
     for (int s = 0; s < kStages - 1; ++s) {
         if (s < nslab) {
@@ -164,7 +182,10 @@ __device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, uint3
         }
         cp_async_commit();
         const uint32_t* st = smem + (kb % kStages) * kQStageWords;
-        q_relax_slab(c, st, st + kQSlabA, tx, ty, one);
+        if (mode == 2)
+            q_relax_slab<8>(c, st, st + kQSlabA, tx, ty, one);
+        else if (mode == 1)
+            q_relax_slab<4>(c, st, st + kQSlabA, tx, ty, one);
     }
     cp_async_wait<0>();
 }
@@ -241,58 +262,102 @@ struct QProof {
     unsigned rmax;  // largest result below CAP
 };
 
-// W = encode(G) for an n x n int32 graph at G (row-major, rows need not be
-// aligned); W has `ld` values (ld / 2 words) per row and ld rows, padding CAP.
-__device__ __forceinline__ void q_encode(const int* __restrict__ G, int n, uint32_t* Wm, int ld, QProof* pf, int tid) {
-    unsigned bad = 0, wmax = 0;
-    const int vecs = ld / 8;  // 8 values (4 words) per step
-    for (int q = tid; q < ld * vecs; q += kThreads) {
-        const int i = q / vecs, j0 = (q % vecs) * 8;
-        uint32_t e[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int j = j0 + u;
-            uint32_t x = kQCap;
-            if (i < n && j < n) {
-                const int v = G[(int64_t)i * n + j];
-                if (v != kInf) {
-                    if (v >= 0 && (uint32_t)v < kQCap) {
-                        x = (uint32_t)v;
-                        wmax = max(wmax, x);
-                    } else {
-                        bad = 1;
-                    }
-                }
-            }
-            e[u] = x;
-        }
-        *reinterpret_cast<uint4*>(Wm + (int64_t)i * (ld / 2) + j0 / 2) =
-            make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+// The per-graph passes below give each warp whole rows and each lane
+// consecutive columns (coalesced accesses to the graph's unaligned int32
+// rows), with kQPassU independent loads per lane in flight.
+constexpr int kQPassU = 4;
+
+__device__ __forceinline__ uint32_t q_encode1(int v, unsigned& bad, unsigned& wmax) {
+    if (v == kInf) return kQCap;
+    if (v >= 0 && (uint32_t)v < kQCap) {
+        wmax = max(wmax, (uint32_t)v);
+        return (uint32_t)v;
     }
-    if (bad) atomicOr(&pf->bad, 1u);
-    if (wmax) atomicMax(&pf->wmax, wmax);
+    bad = 1;
+    return kQCap;
 }
 
-// Largest result below CAP over the graph's n x n entries.
-__device__ __forceinline__ void q_rmax(const uint32_t* Wm, int n, int ld, QProof* pf, int tid) {
-    unsigned m = 0;
-    const int words = (n + 1) / 2;
-    for (int q = tid; q < n * words; q += kThreads) {
-        const int i = q / words, w = q % words;
-        const uint32_t x = Wm[(int64_t)i * (ld / 2) + w];
-        const uint32_t lo = x & 0xFFFFu, hi = x >> 16;
-        if (lo < kQCap) m = max(m, lo);
-        if (2 * w + 1 < n && hi < kQCap) m = max(m, hi);
+// W = encode(G) for an n x n int32 graph at G (row-major, rows need not be
+// aligned); W has `ld` values (ld / 2 words) per row and ld rows, padding CAP.
+__device__ __forceinline__ void q_encode(const int* __restrict__ G, int n, uint32_t* __restrict__ Wm, int ld,
+                                         QProof* pf) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ldw = ld / 2;
+    unsigned bad = 0, wmax = 0;
+    for (int i = warp; i < ld; i += kThreads / 32) {
+        const int* row = G + (int64_t)i * n;
+        for (int jw0 = 0; jw0 < ldw; jw0 += 32 * kQPassU) {
+            int v[kQPassU][2];
+#pragma unroll
+            for (int u = 0; u < kQPassU; ++u) {
+                const int j = 2 * (jw0 + u * 32 + lane);
+                v[u][0] = (i < n && j < n) ? __ldg(row + j) : kInf;
+                v[u][1] = (i < n && j + 1 < n) ? __ldg(row + j + 1) : kInf;
+            }
+#pragma unroll
+            for (int u = 0; u < kQPassU; ++u) {
+                const int jw = jw0 + u * 32 + lane;
+                if (jw < ldw)
+                    Wm[(int64_t)i * ldw + jw] = q_encode1(v[u][0], bad, wmax) | (q_encode1(v[u][1], bad, wmax) << 16);
+            }
+        }
     }
-    if (m) atomicMax(&pf->rmax, m);
+    for (int o = 16; o > 0; o >>= 1) {
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+        wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    }
+    if (lane == 0) {
+        if (bad) atomicOr(&pf->bad, 1u);
+        if (wmax) atomicMax(&pf->wmax, wmax);
+    }
+}
+
+// Largest result below CAP over the graph's rows (padding is CAP and never
+// counts), 16-byte loads.
+__device__ __forceinline__ void q_rmax(const uint32_t* __restrict__ Wm, int n, int ld, QProof* pf) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ldw = ld / 2;
+    unsigned m = 0;
+    for (int i = warp; i < n; i += kThreads / 32) {
+        const uint32_t* row = Wm + (int64_t)i * ldw;
+        for (int w0 = lane * 4; w0 < ldw; w0 += 128) {
+            const uint4 x = *reinterpret_cast<const uint4*>(row + w0);
+            const uint32_t ws[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t lo = ws[e] & 0xFFFFu, hi = ws[e] >> 16;
+                if (lo < kQCap) m = max(m, lo);
+                if (hi < kQCap) m = max(m, hi);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m) atomicMax(&pf->rmax, m);
 }
 
 // G = decode(W) (CAP -> INF) for the graph's n x n entries.
-__device__ __forceinline__ void q_decode(const uint32_t* Wm, int* __restrict__ G, int n, int ld, int tid) {
-    for (int q = tid; q < n * n; q += kThreads) {
-        const int i = q / n, j = q % n;
-        const uint32_t x = (Wm[(int64_t)i * (ld / 2) + (j >> 1)] >> ((j & 1) * 16)) & 0xFFFFu;
-        G[q] = (x == kQCap) ? kInf : (int)x;
+__device__ __forceinline__ void q_decode(const uint32_t* __restrict__ Wm, int* __restrict__ G, int n, int ld) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ldw = ld / 2;
+    for (int i = warp; i < n; i += kThreads / 32) {
+        const uint32_t* wrow = Wm + (int64_t)i * ldw;
+        int* row = G + (int64_t)i * n;
+        for (int j0 = 0; j0 < n; j0 += 32 * kQPassU) {
+            uint32_t x[kQPassU];
+#pragma unroll
+            for (int u = 0; u < kQPassU; ++u) {
+                const int j = j0 + u * 32 + lane;
+                x[u] = (j < n) ? wrow[j >> 1] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < kQPassU; ++u) {
+                const int j = j0 + u * 32 + lane;
+                if (j < n) {
+                    const uint32_t v = (x[u] >> ((j & 1) * 16)) & 0xFFFFu;
+                    row[j] = (v == kQCap) ? kInf : (int)v;
+                }
+            }
+        }
     }
 }
 
@@ -339,7 +404,7 @@ __device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* c
             const int64_t w0 = (int64_t)tj * kQTileW;
             q_load_tile(c, Wm, ldw, p0, w0, tx, ty);
             q_mainloop(
-                c, nslab, smem,
+                c, nslab, kv, smem,
                 [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, p0, tid); },
                 [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, Wm, ldw, p0 + s * kSlab, w0, tid); },
                 tx, ty, one);
@@ -353,7 +418,7 @@ __device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* c
             const int64_t r0 = (int64_t)ti * kTile;
             q_load_tile(c, Wm, ldw, r0, pw0, tx, ty);
             q_mainloop(
-                c, nslab, smem,
+                c, nslab, min(kTile, n - (int)r0), smem,
                 [&](uint32_t* dst, int s) { q_load_transposed_dup(dst, Wm, ldw, r0, pw0 + s * (kSlab / 2), tid); },
                 [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, pw0, tid); },
                 tx, ty, one);
@@ -384,7 +449,7 @@ __device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* c
                 const int64_t w0 = (int64_t)tj * kQTileW;
                 q_load_tile(c, Wm, ldw, r0, w0, tx, ty);
                 q_mainloop(
-                    c, nslab, smem,
+                    c, nslab, min(kTile, n - (int)r0), smem,
                     [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, r0, tid); },
                     [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, w0, tid); },
                     tx, ty, one);

@@ -270,17 +270,17 @@ __global__ void __launch_bounds__(kThreads, 2)
         uint32_t* colD = Wm + (int64_t)ld * (ld / 2);
         uint32_t* rowP = colD + (int64_t)kTile * ld;
         int* G = packed + item.offset;
-        q_encode(G, n, Wm, ld, &pf, tid);
+        q_encode(G, n, Wm, ld, &pf);
         __syncthreads();
         bool take = pf.bad == 0;
         if (take) {
             q_sweep(Wm, n, ld, colD, rowP, qsm, one);
-            q_rmax(Wm, n, ld, &pf, tid);
+            q_rmax(Wm, n, ld, &pf);
             __syncthreads();
             take = pf.rmax + pf.wmax < kQCap;
         }
         if (take) {
-            q_decode(Wm, G, n, ld, tid);
+            q_decode(Wm, G, n, ld);
         } else if (tid == 0) {
             fallback[atomicAdd(&counters[kFallbackCount], 1)] = start + it;
         }

@@ -8,6 +8,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -91,3 +92,18 @@ def test_dijkstra_rows_checker(oracle):
     rows[17][3] += 1  # a wrong entry in the result under test is caught
     r = bench.dijkstra_rows(W, rows, 2)
     assert r["rows_vs_dijkstra"] == "2/3" and not r["all_rows_match"]
+
+
+def test_batched_sample_checker(oracle):
+    rng = np.random.default_rng(0)
+    sizes = rng.integers(1, 40, 20).astype(np.int32)
+    offsets = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)[:-1]])
+    packed = np.concatenate([oracle.generate_graph(int(n), 0.5, 100 + g, 1, 9).ravel() for g, n in enumerate(sizes)])
+    out = np.concatenate([oracle.fw_i32(packed[o:o + n * n].reshape(n, n)).ravel()
+                          for n, o in zip(sizes.tolist(), offsets.tolist())])
+    r = bench.batched_sample_check((sizes, offsets, packed, out), 12, 2)
+    assert r["batched_graphs_vs_oracle"] == "12/12" and r["batched_all_match"]
+    g = int(np.argmax(sizes))  # always sampled (among the 8 largest)
+    out[int(offsets[g])] += 1  # a wrong entry in the result under test is caught
+    r = bench.batched_sample_check((sizes, offsets, packed, out), 12, 2)
+    assert r["batched_graphs_vs_oracle"] == "11/12" and not r["batched_all_match"]
