@@ -15,18 +15,23 @@
 //   bit; otherwise the graph is left untouched and handed to the int32 path.
 //
 // The CTA (256 threads) keeps the graph's 16-bit copy W (leading dimension
-// ld = n rounded up to 128 values, padded with CAP) in its workspace slice,
-// with the current pivot block's panels: colD[k][i] = D[i][p0 + k] duplicated
-// into both halves of a word (the A operand of the packed add-min), rowP[k][*]
-// = row p0 + k as packed words (the B operand). Per 128-wide pivot block:
-// the closure of the diagonal block in registers, the row panel min(R, Dg* x R)
-// and the column panel min(C, C x Dg*) (plain min-plus products, Dg* being
-// closed), then the remainder min(D, C x R), tile after tile. A tile is 128
-// rows x 128 values = 64 words; each thread holds 8 rows x 4 words (16 bytes
-// per row) and folds pivot pairs as the single-graph kernels do: two packed
-// DPX add-mins (form A) or two 32-bit multiply-adds by a runtime 1 on the FMA
-// pipe plus one packed three-way DPX min (form B; exact because every half is
-// at most CAP, so no carry crosses into the other half).
+// ld = n rounded up to 128 values, padded with CAP) in its workspace slice;
+// nothing else of the graph lives in global memory. Per 128-wide pivot block
+// P: the closure of the diagonal block in registers; then the row panel
+// min(R, Dg* x R) and, tile row after tile row, the column panel
+// min(C, C x Dg*) and the remainder min(D, C x R) (plain min-plus products,
+// Dg* being closed). The A operand of a product (128 rows x 128 pivots, each
+// value duplicated into both halves of a word for the packed add-min) stays
+// resident in shared memory for every tile that uses it: Dg* for the row
+// panel, the tile row's pre-update column panel for its own product, then
+// its updated column panel for the tile row's remainder tiles. The B operand
+// (the pivot rows, packed words) streams from W's rows of P in 32-pivot
+// slabs through a three-stage cp.async ring. A tile is 128 rows x 128 values
+// = 64 words; each thread holds 8 rows x 4 words (16 bytes per row) and folds
+// pivot pairs as the single-graph kernels do: two packed DPX add-mins
+// (form A) or two 32-bit multiply-adds by a runtime 1 on the FMA pipe plus
+// one packed three-way DPX min (form B; exact because every half is at most
+// CAP, so no carry crosses into the other half).
 #pragma once
 
 #include <cstdint>
@@ -39,18 +44,24 @@ namespace fw {
 constexpr uint32_t kQCap = 0x7FFF;
 constexpr int kQMaxN = 1024;                          // largest graph the packed batched path takes
 constexpr int kQTileW = kTile / 2;                    // tile width in words
-constexpr int kQSlabA = kSlab * kTile;                // words: 32 pivots x 128 rows (duplicated values)
+constexpr int kQPanelWords = kTile * kTile;           // resident A: 128 pivots x 128 rows (duplicated values)
 constexpr int kQSlabB = kSlab * kQTileW;              // words: 32 pivots x 64 words
-constexpr int kQStageWords = kQSlabA + kQSlabB;
-constexpr int kQSmemBytes = kStages * kQStageWords * 4;  // 72 KB
+constexpr int kQSmemBytes = (kQPanelWords + kStages * kQSlabB) * 4;  // 64 KB + 24 KB
 // Words (bit w of the thread's 4) that take form A: {1, 2} (the batched
 // workload in 3.67 ms; {0, 2} 3.72, {0, 1} 3.71, {1, 3} 3.70, {0, 3} 3.74,
 // {0} 3.78, {1, 2, 3} 3.72 ms).
 constexpr unsigned kQWordsA = 0x6u;
 
 // Workspace words of one CTA for graphs up to `ld` values wide (ld a
-// multiple of 128): W, colD (128 x ld), rowP (128 x ld / 2).
-__host__ __device__ inline int64_t q_ws_words(int64_t ld) { return ld * (ld / 2) + (int64_t)kTile * ld + (int64_t)kTile * (ld / 2); }
+// multiple of 128): the graph's 16-bit copy.
+__host__ __device__ inline int64_t q_ws_words(int64_t ld) { return ld * (ld / 2); }
+
+// The resident A panel holds A[k][i] (pivot k, tile row i) at
+// k * 128 + (i ^ q_swz(k)): rows of eight pivots are XOR-swizzled in 16-byte
+// chunks, so that the transposed stores from registers (threads of a warp
+// writing pivots 8 apart) spread over the banks, while every thread's
+// 16-byte reads of four consecutive rows stay aligned.
+__device__ __forceinline__ int q_swz(int k) { return ((k >> 3) & 7) << 2; }
 
 __device__ __forceinline__ uint32_t q_dup(uint32_t v) { return v | (v << 16); }
 
@@ -63,37 +74,60 @@ __device__ __forceinline__ uint32_t q_relax2(bool form_a, uint32_t acc, uint32_t
     return __vimin3_u16x2(acc, s0, s1);
 }
 
-// acc = min(acc, A (x) B) over one 32-pivot slab in shared memory: A k-major
-// [32][128] duplicated words (rows of the tile), B k-major [32][64] words.
-// NR = 8: all of the thread's rows; NR = 4: its first four (rows 64.. of the
-// tile lie outside the graph).
+// acc = min(acc, A (x) B) over the 32 pivots [k0, k0 + 32): A the resident
+// panel, B a k-major [32][64] slab of packed words. NR = 8: all of the
+// thread's rows; NR = 4: its first four (rows 64.. of the tile lie outside
+// the graph). The swizzle is constant over groups of eight pivots.
 template <int NR>
-__device__ __forceinline__ void q_relax_slab(uint32_t (&c)[8][4], const uint32_t* As, const uint32_t* Bs, int tx,
-                                             int ty, int one) {
+__device__ __forceinline__ void q_relax_slab(uint32_t (&c)[8][4], const uint32_t* Ap, int k0, const uint32_t* Bs,
+                                             int tx, int ty, int one) {
 #pragma unroll 1
-    for (int kk = 0; kk < kSlab; kk += 2) {
-        uint32_t a0[8], a1[8], b0[4], b1[4];
-        {
-            const uint4 l0 = *reinterpret_cast<const uint4*>(As + kk * kTile + ty * 4);
-            const uint4 l1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + ty * 4);
-            const uint4 q0 = *reinterpret_cast<const uint4*>(Bs + kk * kQTileW + tx * 4);
-            const uint4 q1 = *reinterpret_cast<const uint4*>(Bs + (kk + 1) * kQTileW + tx * 4);
+    for (int g = 0; g < kSlab; g += 8) {
+        const int swz = q_swz(k0 + g);
+        const uint32_t* A8 = Ap + (k0 + g) * kTile;
+        const int lo = (ty * 4) ^ swz, hi = (64 + ty * 4) ^ swz;
+#pragma unroll
+        for (int kk = 0; kk < 8; kk += 2) {
+            uint32_t a0[8], a1[8], b0[4], b1[4];
+            const uint4 l0 = *reinterpret_cast<const uint4*>(A8 + kk * kTile + lo);
+            const uint4 l1 = *reinterpret_cast<const uint4*>(A8 + (kk + 1) * kTile + lo);
+            const uint4 q0 = *reinterpret_cast<const uint4*>(Bs + (g + kk) * kQTileW + tx * 4);
+            const uint4 q1 = *reinterpret_cast<const uint4*>(Bs + (g + kk + 1) * kQTileW + tx * 4);
             a0[0] = l0.x; a0[1] = l0.y; a0[2] = l0.z; a0[3] = l0.w;
             a1[0] = l1.x; a1[1] = l1.y; a1[2] = l1.z; a1[3] = l1.w;
             if (NR == 8) {
-                const uint4 h0 = *reinterpret_cast<const uint4*>(As + kk * kTile + 64 + ty * 4);
-                const uint4 h1 = *reinterpret_cast<const uint4*>(As + (kk + 1) * kTile + 64 + ty * 4);
+                const uint4 h0 = *reinterpret_cast<const uint4*>(A8 + kk * kTile + hi);
+                const uint4 h1 = *reinterpret_cast<const uint4*>(A8 + (kk + 1) * kTile + hi);
                 a0[4] = h0.x; a0[5] = h0.y; a0[6] = h0.z; a0[7] = h0.w;
                 a1[4] = h1.x; a1[5] = h1.y; a1[6] = h1.z; a1[7] = h1.w;
             }
             b0[0] = q0.x; b0[1] = q0.y; b0[2] = q0.z; b0[3] = q0.w;
             b1[0] = q1.x; b1[1] = q1.y; b1[2] = q1.z; b1[3] = q1.w;
+#pragma unroll
+            for (int r = 0; r < NR; ++r)
+#pragma unroll
+                for (int w = 0; w < 4; ++w)
+                    c[r][w] = q_relax2(((kQWordsA >> w) & 1u) != 0, c[r][w], a0[r], b0[w], a1[r], b1[w], one);
         }
+    }
+}
+
+// The thread's part of the tile held as c, transposed and duplicated into
+// the resident A panel: A[k][i] = dup(value (i, k)) for the tile's rows i and
+// columns k (column k = value 2 * word + half).
+__device__ __forceinline__ void q_store_panel(const uint32_t (&c)[8][4], uint32_t* Ap, int tx, int ty) {
+    const int swz = (tx & 7) << 2;  // q_swz(k) for every k = 8 tx + 0..7
 #pragma unroll
-        for (int r = 0; r < NR; ++r)
+    for (int w = 0; w < 4; ++w) {
 #pragma unroll
-            for (int w = 0; w < 4; ++w)
-                c[r][w] = q_relax2(((kQWordsA >> w) & 1u) != 0, c[r][w], a0[r], b0[w], a1[r], b1[w], one);
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * (tx * 4 + w) + h;
+            uint32_t v[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> (16 * h)) & 0xFFFFu);
+            *reinterpret_cast<uint4*>(Ap + k * kTile + ((ty * 4) ^ swz)) = make_uint4(v[0], v[1], v[2], v[3]);
+            *reinterpret_cast<uint4*>(Ap + k * kTile + ((64 + ty * 4) ^ swz)) = make_uint4(v[4], v[5], v[6], v[7]);
+        }
     }
 }
 
@@ -138,54 +172,30 @@ __device__ __forceinline__ void q_load_kmajor_async(uint32_t* dst, const uint32_
     }
 }
 
-// A slab of the column panel taken from the tile itself: dst[kk][i] =
-// dup(value (r0 + i, p0 + k0 + kk)) for kk < 32, i < 128 (plain loads: each
-// thread reads 8 words of one row and writes 16 duplicated values).
-__device__ __forceinline__ void q_load_transposed_dup(uint32_t* dst, const uint32_t* Wm, int64_t ldw, int64_t r0,
-                                                      int64_t pw0, int tid) {
-    const int i = tid & (kTile - 1), part = tid >> 7;  // 2 threads per row, 8 words each
-    const uint32_t* src = Wm + (r0 + i) * ldw + pw0 + part * 8;
-    const uint4 x = *reinterpret_cast<const uint4*>(src);
-    const uint4 y = *reinterpret_cast<const uint4*>(src + 4);
-    const uint32_t v[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
-#pragma unroll
-    for (int w = 0; w < 8; ++w) {
-        const int kk = part * 16 + 2 * w;
-        dst[kk * kTile + i] = q_dup(v[w] & 0xFFFFu);
-        dst[(kk + 1) * kTile + i] = q_dup(v[w] >> 16);
-    }
-}
-
-// Three-stage cp.async pipeline over `nslab` slabs (the int32 mainloop's
-// schedule); la / lb fill slab s of A / B. `rows`: the tile's rows inside the
-// graph (see q_row_mode).
-template <class LA, class LB>
-__device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, int rows, uint32_t* smem, LA la, LB lb,
-                                           int tx, int ty, int one) {
+// acc = min(acc, A (x) B) over `nslab` slabs: A the resident panel, B
+// streamed through a three-stage cp.async ring (the int32 mainloop's
+// schedule); lb fills slab s of B. `rows`: the tile's rows inside the graph
+// (see q_row_mode).
+template <class LB>
+__device__ __forceinline__ void q_mainloop(uint32_t (&c)[8][4], int nslab, int rows, const uint32_t* Ap,
+                                           uint32_t* Bst, LB lb, int tx, int ty, int one) {
     const int mode = q_row_mode(rows);
 #pragma unroll
     for (int s = 0; s < kStages - 1; ++s) {
-        if (s < nslab) {
-            la(smem + s * kQStageWords, s);
-            lb(smem + s * kQStageWords + kQSlabA, s);
-        }
+        if (s < nslab) lb(Bst + s * kQSlabB, s);
         cp_async_commit();
     }
     for (int kb = 0; kb < nslab; ++kb) {
         cp_async_wait<kStages - 2>();
         __syncthreads();
         const int nxt = kb + kStages - 1;
-        if (nxt < nslab) {
-            uint32_t* st = smem + (nxt % kStages) * kQStageWords;
-            la(st, nxt);
-            lb(st + kQSlabA, nxt);
-        }
+        if (nxt < nslab) lb(Bst + (nxt % kStages) * kQSlabB, nxt);
         cp_async_commit();
-        const uint32_t* st = smem + (kb % kStages) * kQStageWords;
+        const uint32_t* Bs = Bst + (kb % kStages) * kQSlabB;
         if (mode == 2)
-            q_relax_slab<8>(c, st, st + kQSlabA, tx, ty, one);
+            q_relax_slab<8>(c, Ap, kb * kSlab, Bs, tx, ty, one);
         else if (mode == 1)
-            q_relax_slab<4>(c, st, st + kQSlabA, tx, ty, one);
+            q_relax_slab<4>(c, Ap, kb * kSlab, Bs, tx, ty, one);
     }
     cp_async_wait<0>();
 }
@@ -362,103 +372,64 @@ __device__ __forceinline__ void q_decode(const uint32_t* __restrict__ Wm, int* _
 }
 
 // The blocked sweep of W (ld x ld values, T = ld / 128 blocks, n valid).
-// colD: 128 x ld duplicated words; rowP: 128 x ld / 2 words.
-__device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* colD, uint32_t* rowP, uint32_t* smem,
-                                        int one) {
+// smem: the resident A panel (kQPanelWords), then the B ring (kStages x
+// kQSlabB words; its start also holds the closure's pivot buffers).
+__device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* smem, int one) {
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int T = ld / kTile;
     const int64_t ldw = ld / 2;
+    uint32_t* Ap = smem;
+    uint32_t* Bst = smem + kQPanelWords;
     for (int pt = 0; pt < T; ++pt) {
         const int p0 = pt * kTile, pw0 = p0 / 2;
         const int kv = min(kTile, n - p0);
         const int nslab = (kv + kSlab - 1) / kSlab;
-        {  // 1. diagonal block: closure in registers, then W, rowP[k][P] and colD[k][P]
-            uint32_t c[8][4];
-            q_load_tile(c, Wm, ldw, p0, pw0, tx, ty);
-            q_close(c, smem, smem + 2 * kQTileW, kv, tx, ty);
-            q_store_tile(c, Wm, ldw, p0, pw0, tx, ty);
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-                *reinterpret_cast<uint4*>(rowP + (int64_t)own_row(ty, r) * ldw + pw0 + tx * 4) =
-                    make_uint4(c[r][0], c[r][1], c[r][2], c[r][3]);
-#pragma unroll
-            for (int w = 0; w < 4; ++w) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int k = 2 * (tx * 4 + w) + h;
-                    uint32_t v[8];
-#pragma unroll
-                    for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> (16 * h)) & 0xFFFFu);
-                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + p0 + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
-                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + p0 + 64 + ty * 4) =
-                        make_uint4(v[4], v[5], v[6], v[7]);
-                }
-            }
-            __threadfence_block();
-            __syncthreads();
-        }
+        // B slabs: rows p0 + 32 s .. of W (the pivot rows), words w0 ..
+        auto pivot_rows = [&](int64_t w0) {
+            return [=](uint32_t* dst, int sl) { q_load_kmajor_async<kQTileW>(dst, Wm, ldw, p0 + sl * kSlab, w0, tid); };
+        };
         uint32_t c[8][4];
-        // 2. row panel: W[P][J] = min(W[P][J], Dg* (x) W[P][J]); rowP[k][J] = result rows
+        // 1. diagonal block: closure in registers; W and the resident A = Dg*
+        q_load_tile(c, Wm, ldw, p0, pw0, tx, ty);
+        q_close(c, Bst, Bst + 2 * kQTileW, kv, tx, ty);
+        q_store_tile(c, Wm, ldw, p0, pw0, tx, ty);
+        q_store_panel(c, Ap, tx, ty);
+        __syncthreads();
+        // 2. row panel: W[P][J] = min(W[P][J], Dg* (x) W[P][J]), B the tile's own
+        //    rows (every thread has read them before the last slab's barrier,
+        //    so the stores after the loop are safe)
         for (int tj = 0; tj < T; ++tj) {
             if (tj == pt) continue;
             const int64_t w0 = (int64_t)tj * kQTileW;
             q_load_tile(c, Wm, ldw, p0, w0, tx, ty);
-            q_mainloop(
-                c, nslab, kv, smem,
-                [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, p0, tid); },
-                [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, Wm, ldw, p0 + s * kSlab, w0, tid); },
-                tx, ty, one);
-            __syncthreads();  // every thread read its B rows (rows of this tile) before any is rewritten
+            q_mainloop(c, nslab, kv, Ap, Bst, pivot_rows(w0), tx, ty, one);
             q_store_tile(c, Wm, ldw, p0, w0, tx, ty);
-            q_store_tile(c, rowP, ldw, 0, w0, tx, ty);
+            __syncthreads();  // the next tile's prologue refills the ring
         }
-        // 3. column panel: W[I][P] = min(W[I][P], W[I][P] (x) Dg*); colD[k][I] = result columns
+        // 3. tile row after tile row
         for (int ti = 0; ti < T; ++ti) {
             if (ti == pt) continue;
             const int64_t r0 = (int64_t)ti * kTile;
+            const int rows = min(kTile, n - (int)r0);
+            // column panel W[I][P] = min(C, C (x) Dg*): A = C (pre-update), B = Dg* rows
             q_load_tile(c, Wm, ldw, r0, pw0, tx, ty);
-            q_mainloop(
-                c, nslab, min(kTile, n - (int)r0), smem,
-                [&](uint32_t* dst, int s) { q_load_transposed_dup(dst, Wm, ldw, r0, pw0 + s * (kSlab / 2), tid); },
-                [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, pw0, tid); },
-                tx, ty, one);
-            __syncthreads();  // every thread read its A columns (of this tile) before any is rewritten
+            q_store_panel(c, Ap, tx, ty);
+            __syncthreads();
+            q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(pw0), tx, ty, one);
+            __syncthreads();  // every thread is done with A = C before it becomes C'
             q_store_tile(c, Wm, ldw, r0, pw0, tx, ty);
-#pragma unroll
-            for (int w = 0; w < 4; ++w) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int k = 2 * (tx * 4 + w) + h;
-                    uint32_t v[8];
-#pragma unroll
-                    for (int r = 0; r < 8; ++r) v[r] = q_dup((c[r][w] >> (16 * h)) & 0xFFFFu);
-                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + r0 + ty * 4) = make_uint4(v[0], v[1], v[2], v[3]);
-                    *reinterpret_cast<uint4*>(colD + (int64_t)k * ld + r0 + 64 + ty * 4) =
-                        make_uint4(v[4], v[5], v[6], v[7]);
-                }
-            }
-        }
-        __threadfence_block();
-        __syncthreads();  // panels complete before the remainder reads them
-        // 4. remainder: W[I][J] = min(W[I][J], colD[:, I]^T (x) rowP[:, J])
-        for (int ti = 0; ti < T; ++ti) {
-            if (ti == pt) continue;
-            const int64_t r0 = (int64_t)ti * kTile;
+            q_store_panel(c, Ap, tx, ty);
+            __syncthreads();
+            // remainder W[I][J] = min(W[I][J], C' (x) W[P][J]), J != P
             for (int tj = 0; tj < T; ++tj) {
                 if (tj == pt) continue;
                 const int64_t w0 = (int64_t)tj * kQTileW;
                 q_load_tile(c, Wm, ldw, r0, w0, tx, ty);
-                q_mainloop(
-                    c, nslab, min(kTile, n - (int)r0), smem,
-                    [&](uint32_t* dst, int s) { q_load_kmajor_async<kTile>(dst, colD, ld, s * kSlab, r0, tid); },
-                    [&](uint32_t* dst, int s) { q_load_kmajor_async<kQTileW>(dst, rowP, ldw, s * kSlab, w0, tid); },
-                    tx, ty, one);
+                q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(w0), tx, ty, one);
                 q_store_tile(c, Wm, ldw, r0, w0, tx, ty);
-                __syncthreads();  // the next tile's prologue refills the ring
+                __syncthreads();  // the next tile's prologue refills the ring; the A panel is rewritten next
             }
         }
-        __threadfence_block();
-        __syncthreads();
     }
 }
 

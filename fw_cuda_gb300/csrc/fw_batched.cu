@@ -267,14 +267,12 @@ __global__ void __launch_bounds__(kThreads, 2)
         const BatchItem item = items[start + it];
         const int n = item.n;
         const int ld = (n + kTile - 1) / kTile * kTile;
-        uint32_t* colD = Wm + (int64_t)ld * (ld / 2);
-        uint32_t* rowP = colD + (int64_t)kTile * ld;
         int* G = packed + item.offset;
         q_encode(G, n, Wm, ld, &pf);
         __syncthreads();
         bool take = pf.bad == 0;
         if (take) {
-            q_sweep(Wm, n, ld, colD, rowP, qsm, one);
+            q_sweep(Wm, n, ld, qsm, one);
             q_rmax(Wm, n, ld, &pf);
             __syncthreads();
             take = pf.rmax + pf.wmax < kQCap;
