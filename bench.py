@@ -796,8 +796,9 @@ def run_reference(args) -> None:
 
 
 def reference_gpu(args, W: np.ndarray, timed: int = 3):
-    """The reference's multi_layer_tiling_gpu kernels (the run's kappa), built
-    for sm_103a from its sources and launched by its own launch loop on the
+    """The reference's kernels of the run's algorithm (`--algorithm`;
+    multi_layer_tiling_gpu for "auto", with the run's kappa), built for
+    sm_103a from its sources and launched by its own launch loop on the
     legacy default stream, on the full workload: one untimed full-size solve,
     then `timed` solves of a fresh copy of the input, each bracketed by CUDA
     events on that stream (the reference's Timer::measureGPU also times one
@@ -810,6 +811,9 @@ def reference_gpu(args, W: np.ndarray, timed: int = 3):
         if not torch.cuda.is_available() or not O.refgpu_available():
             return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
         n = W.shape[0]
+        algo = args.algorithm if args.algorithm in ("baseline_gpu", "tiling_gpu") else "multi_layer_tiling_gpu"
+        source = {"baseline_gpu": "src/fw_baseline_gpu.cu", "tiling_gpu": "src/fw_tiling_gpu.cu",
+                  "multi_layer_tiling_gpu": "src/fw_multi_layer_tiling_gpu.cu"}[algo]
         legacy = torch.cuda.default_stream()
         pristine = torch.from_numpy(W).cuda()
         d = torch.empty_like(pristine)
@@ -820,16 +824,16 @@ def reference_gpu(args, W: np.ndarray, timed: int = 3):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(legacy)
-            O.refgpu_run("multi_layer_tiling_gpu", d.data_ptr(), n, args.kappa)  # synchronises the context
+            O.refgpu_run(algo, d.data_ptr(), n, args.kappa)  # synchronises the context
             b.record(legacy)
             b.synchronize()
             if i > 0:
                 secs.append(a.elapsed_time(b) / 1e3)
         mean = sum(secs) / len(secs)
-        return {"algorithm": "multi_layer_tiling_gpu", "kappa": args.kappa, "value": float(n) ** 3 / mean,
+        return {"algorithm": algo, "kappa": args.kappa, "value": float(n) ** 3 / mean,
                 "unit": UNIT, "seconds_per_solve": mean, "seconds_min": min(secs), "seconds_max": max(secs),
                 "solves_timed": len(secs),
-                "how": "reference kernels (src/fw_multi_layer_tiling_gpu.cu) compiled for sm_103a, launched by the "
+                "how": f"reference kernels ({source}) compiled for sm_103a, launched by the "
                        "reference launch loop on the legacy default stream; one full-size warm-up solve, then "
                        "CUDA events around each timed solve of a fresh copy of the input"}
     except Exception as e:  # report, never fail the CPU line
