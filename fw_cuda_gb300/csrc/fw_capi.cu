@@ -47,6 +47,7 @@ struct ProfState {
         int kc;
         cudaEvent_t a, b;
         double relax;
+        int64_t launches;
     };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> open;  // one pending start event per class
@@ -87,14 +88,14 @@ void prof_begin(KernelClass kc, cudaStream_t s) {
     g_prof.open[kc] = e;
 }
 
-void prof_end(KernelClass kc, cudaStream_t s, double relaxations) {
+void prof_end(KernelClass kc, cudaStream_t s, double relaxations, int64_t launches) {
     if (!g_prof.on) return;
     std::lock_guard<std::mutex> lk(g_prof_mutex);
     cudaEvent_t a = g_prof.open[kc];
     cudaEvent_t b = prof_event();
     if (!a || !b) return;
     cudaEventRecord(b, s);
-    g_prof.recs.push_back({kc, a, b, relaxations});
+    g_prof.recs.push_back({kc, a, b, relaxations, launches});
     g_prof.open[kc] = nullptr;
 }
 
@@ -456,7 +457,7 @@ int fw_profile_end(fw_kernel_stats* out, int cap, int* count) {
             status = cuda_error(cudaGetLastError(), "cudaEventElapsedTime");
             continue;
         }
-        agg[r.kc].launches += 1;
+        agg[r.kc].launches += r.launches;
         agg[r.kc].total_ms += ms;
         agg[r.kc].relaxations += r.relax;
     }

@@ -70,7 +70,9 @@ enum KernelClass {
 // Brackets one launch with events when profiling is on (no-ops otherwise).
 // `relaxations` is the algorithmic work the launch performs.
 void prof_begin(KernelClass kc, cudaStream_t s);
-void prof_end(KernelClass kc, cudaStream_t s, double relaxations);
+// `launches`: the kernel launches the bracket stands for (a replayed graph
+// of several counts them all).
+void prof_end(KernelClass kc, cudaStream_t s, double relaxations, int64_t launches = 1);
 
 // Every workspace of an asynchronous sweep entry point starts with a status
 // block of this size; its first word counts the call's tile copies that
