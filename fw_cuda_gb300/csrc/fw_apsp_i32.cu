@@ -635,8 +635,8 @@ int pivot_graph_launch(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
 
 }  // namespace
 
-int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s) {
-    if (n >= kPivotGraphMinN && n <= kPivotGraphMaxN) {
+int pivot_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, bool may_allocate) {
+    if (may_allocate && n >= kPivotGraphMinN && n <= kPivotGraphMaxN) {
         cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
         FW_CUDA_TRY(cudaStreamIsCapturing(s, &st));
         if (st == cudaStreamCaptureStatusNone) return pivot_graph_launch(D, n, ws, s);

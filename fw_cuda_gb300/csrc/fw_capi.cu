@@ -259,12 +259,9 @@ size_t min_workspace_bytes(int64_t n, int kappa, int variant) {
         return kStatusBytes + ((blocked_workspace_bytes(n, 2) + 255) & ~size_t(255)) + p16_workspace_bytes(n);
     return kStatusBytes + blocked;
 }
-}  // namespace fw
 
-extern "C" {
-
-int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
-                   size_t workspace_bytes, fw_stream_t stream) {
+int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
+                size_t workspace_bytes, fw_stream_t stream, bool may_allocate) {
     if (int rc = check_apsp_args(d_D, n, variant)) return rc;
     (void)tile;  // fixed geometry, as in the reference (src/fw_tiling_gpu.cu:254-257)
     const size_t need = min_workspace_bytes(n, kappa, variant);
@@ -284,7 +281,7 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
     if (int rc = status_begin(s, status)) return rc;
     int rc = FW_OK;
     if (variant == FW_VARIANT_BASELINE) {
-        rc = pivot_solve(d_D, n, body, s);
+        rc = pivot_solve(d_D, n, body, s, may_allocate);
     } else if (variant == FW_VARIANT_AUTO) {
         const size_t blocked = (blocked_workspace_bytes(n, 2) + 255) & ~size_t(255);
         const unsigned int* done = nullptr;
@@ -305,6 +302,14 @@ int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, vo
     }
     if (rc) return rc;
     return status_end(s, status);
+}
+}  // namespace fw
+
+extern "C" {
+
+int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
+                   size_t workspace_bytes, fw_stream_t stream) {
+    return apsp_i32_ws(d_D, n, tile, kappa, variant, d_workspace, workspace_bytes, stream, true);
 }
 
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream) {

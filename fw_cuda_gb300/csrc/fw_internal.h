@@ -135,7 +135,12 @@ size_t p16_workspace_bytes(int64_t n);
 int p16_solve(int32_t* D, int64_t n, void* ws, cudaStream_t s, const unsigned int** done_flag,
               bool inject_copy_fault = false);
 size_t pivot_workspace_bytes(int64_t n);
-int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s);
+// may_allocate = false: plain launches only (no CUDA graph is captured,
+// which would allocate driver resources).
+int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s, bool may_allocate = true);
+// fw_apsp_i32_ws; may_allocate = false for callers that must allocate nothing.
+int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
+                size_t workspace_bytes, fw_stream_t stream, bool may_allocate);
 
 // Differentiable fp32 forward / backward (fw_diff.cu).
 size_t f32_workspace_bytes(int64_t n, int64_t batch);

@@ -126,6 +126,7 @@ extern "C" int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa,
     // An earlier AUTO report of this stream no longer describes its last call.
     if (was_auto) fw::forget_auto_report(reinterpret_cast<cudaStream_t>(stream));
     // Passing exactly the minimum keeps the single-stream schedule (the
-    // look-ahead would also create a side stream on first use).
-    return fw_apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, need, stream);
+    // look-ahead would also create a side stream on first use), and the
+    // per-pivot sweep launches directly instead of replaying a graph.
+    return fw::apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, need, stream, false);
 }

@@ -46,20 +46,22 @@ def test_noalloc_rejects_graphs_beyond_its_scratch(fw, cuda):
     assert b"8192" in fw.lib().fw_last_error_string()
 
 
-def test_noalloc_allocates_no_device_memory(fw, cuda):
+@pytest.mark.parametrize("n,variant", [(8192, 2), (1024, 0)])
+def test_noalloc_allocates_no_device_memory(fw, cuda, n, variant):
     """The defining property: once the library is loaded (the first call looks
     up the array, which loads the module that holds it), a call on a stream
-    the library has never seen leaves the device's free memory unchanged."""
+    the library has never seen leaves the device's free memory unchanged. At
+    n = 1024 the allocating entry point would replay the per-pivot sweep from
+    a captured CUDA graph; this one must launch directly."""
     f = _noalloc(fw)
-    n = 8192
     W = fw.generate_graph(n, 0.3, 77, 1, 100)
     d = cuda.from_numpy(W).cuda()
     warm = cuda.from_numpy(W).cuda()
-    assert f(warm.data_ptr(), n, 32, 4, 2, None) == fw.FW_OK
+    assert f(warm.data_ptr(), n, 32, 4, variant, None) == fw.FW_OK
     cuda.cuda.synchronize()
     s = cuda.cuda.Stream()
     free_before, _ = cuda.cuda.mem_get_info()
-    rc = f(d.data_ptr(), n, 32, 4, 2, s.cuda_stream)
+    rc = f(d.data_ptr(), n, 32, 4, variant, s.cuda_stream)
     assert rc == fw.FW_OK, fw.lib().fw_last_error_string()
     s.synchronize()
     free_after, _ = cuda.cuda.mem_get_info()
