@@ -14,9 +14,15 @@
 //   gives the int32 sweep's result (src/fw_baseline_cpu.cpp:6-15) bit for
 //   bit; otherwise the graph is left untouched and handed to the int32 path.
 //
-// The CTA (256 threads) keeps the graph's 16-bit copy W (leading dimension
-// ld = n rounded up to 128 values, padded with CAP) in its workspace slice;
-// nothing else of the graph lives in global memory. Per 128-wide pivot block
+// The CTA (256 threads) keeps two 16-bit copies of the graph (leading
+// dimension ld = n rounded up to 128 values, padded with CAP) in its
+// workspace slice: E, the encoded input, and S, the matrix being swept. The
+// first pivot block reads its tiles from E and writes them to S; later
+// blocks work in S; the last block writes every tile, final, decoded
+// (CAP -> INF) straight into the int32 graph and takes the largest result
+// below CAP from registers. E stays as the input was, so a graph that fails
+// the proof is restored from it before it is handed to the int32 path.
+// Per 128-wide pivot block
 // P: the closure of the diagonal block in registers; then the row panel
 // min(R, Dg* x R) and, tile row after tile row, the column panel
 // min(C, C x Dg*) and the remainder min(D, C x R) (plain min-plus products,
@@ -52,9 +58,10 @@ constexpr int kQSmemBytes = (kQPanelWords + kStages * kQSlabB) * 4;  // 64 KB + 
 // {0} 3.78, {1, 2, 3} 3.72 ms).
 constexpr unsigned kQWordsA = 0x6u;
 
-// Workspace words of one CTA for graphs up to `ld` values wide (ld a
-// multiple of 128): the graph's 16-bit copy.
-__host__ __device__ inline int64_t q_ws_words(int64_t ld) { return ld * (ld / 2); }
+// Words of one 16-bit copy of a graph `ld` values wide (ld a multiple of
+// 128); a CTA's workspace slice holds two (E and S) for the largest graph.
+__host__ __device__ inline int64_t q_copy_words(int64_t ld) { return ld * (ld / 2); }
+__host__ __device__ inline int64_t q_ws_words(int64_t ld) { return 2 * q_copy_words(ld); }
 
 // The resident A panel holds A[k][i] (pivot k, tile row i) at
 // k * 128 + (i ^ q_swz(k)): rows of eight pivots are XOR-swizzled in 16-byte
@@ -157,6 +164,48 @@ __device__ __forceinline__ void q_store_tile(const uint32_t (&c)[8][4], uint32_t
     for (int r = 0; r < 8; ++r)
         *reinterpret_cast<uint4*>(Wm + (r0 + own_row(ty, r)) * ldw + w0 + tx * 4) =
             make_uint4(c[r][0], c[r][1], c[r][2], c[r][3]);
+}
+
+// The thread's 8 rows x 8 values of the tile at (r0, word w0), final:
+// decoded (CAP -> INF) into the n x n int32 graph G (rows of n values, any
+// alignment; rows and columns past n are padding and skipped), and
+// m = max(m, every value below CAP). Padding is CAP throughout the sweep, so
+// it never counts.
+__device__ __forceinline__ void q_store_tile_i32(const uint32_t (&c)[8][4], int* __restrict__ G, int n, int r0,
+                                                 int w0, int tx, int ty, unsigned& m) {
+    const int col0 = 2 * (w0 + tx * 4);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        int v[8];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t lo = c[r][w] & 0xFFFFu, hi = c[r][w] >> 16;
+            if (lo < kQCap) m = max(m, lo);
+            if (hi < kQCap) m = max(m, hi);
+            v[2 * w] = lo == kQCap ? kInf : (int)lo;
+            v[2 * w + 1] = hi == kQCap ? kInf : (int)hi;
+        }
+        const int row = r0 + own_row(ty, r);
+        if (row >= n) continue;
+        int* p = G + (int64_t)row * n + col0;
+        if (col0 + 8 <= n) {
+            const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+            if ((a & 15) == 0) {
+                reinterpret_cast<int4*>(p)[0] = make_int4(v[0], v[1], v[2], v[3]);
+                reinterpret_cast<int4*>(p)[1] = make_int4(v[4], v[5], v[6], v[7]);
+            } else if ((a & 7) == 0) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) reinterpret_cast<int2*>(p)[e] = make_int2(v[2 * e], v[2 * e + 1]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) p[e] = v[e];
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                if (col0 + e < n) p[e] = v[e];
+        }
+    }
 }
 
 // k-major slab [32][width] words from rows k0.. of a buffer with `ld` words
@@ -322,30 +371,8 @@ __device__ __forceinline__ void q_encode(const int* __restrict__ G, int n, uint3
     }
 }
 
-// Largest result below CAP over the graph's rows (padding is CAP and never
-// counts), 16-byte loads.
-__device__ __forceinline__ void q_rmax(const uint32_t* __restrict__ Wm, int n, int ld, QProof* pf) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ldw = ld / 2;
-    unsigned m = 0;
-    for (int i = warp; i < n; i += kThreads / 32) {
-        const uint32_t* row = Wm + (int64_t)i * ldw;
-        for (int w0 = lane * 4; w0 < ldw; w0 += 128) {
-            const uint4 x = *reinterpret_cast<const uint4*>(row + w0);
-            const uint32_t ws[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const uint32_t lo = ws[e] & 0xFFFFu, hi = ws[e] >> 16;
-                if (lo < kQCap) m = max(m, lo);
-                if (hi < kQCap) m = max(m, hi);
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0 && m) atomicMax(&pf->rmax, m);
-}
-
-// G = decode(W) (CAP -> INF) for the graph's n x n entries.
+// G = decode(W) (CAP -> INF) for the graph's n x n entries: restores the
+// input from E when a graph fails the proof.
 __device__ __forceinline__ void q_decode(const uint32_t* __restrict__ Wm, int* __restrict__ G, int n, int ld) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ldw = ld / 2;
@@ -371,66 +398,84 @@ __device__ __forceinline__ void q_decode(const uint32_t* __restrict__ Wm, int* _
     }
 }
 
-// The blocked sweep of W (ld x ld values, T = ld / 128 blocks, n valid).
+// The blocked sweep of the graph (ld x ld values, T = ld / 128 blocks, n
+// valid): the first block reads E and writes S, later blocks read and write
+// S, and the last block writes its tiles into G (int32) instead, except the
+// diagonal block and the row panel, which its later steps read as B and so
+// also go to S. Returns the thread's largest result below CAP.
 // smem: the resident A panel (kQPanelWords), then the B ring (kStages x
 // kQSlabB words; its start also holds the closure's pivot buffers).
-__device__ __forceinline__ void q_sweep(uint32_t* Wm, int n, int ld, uint32_t* smem, int one) {
+__device__ __forceinline__ unsigned q_sweep(const uint32_t* E, uint32_t* S, int* G, int n, int ld, uint32_t* smem,
+                                            int one) {
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int T = ld / kTile;
     const int64_t ldw = ld / 2;
     uint32_t* Ap = smem;
     uint32_t* Bst = smem + kQPanelWords;
+    unsigned m = 0;
     for (int pt = 0; pt < T; ++pt) {
         const int p0 = pt * kTile, pw0 = p0 / 2;
         const int kv = min(kTile, n - p0);
         const int nslab = (kv + kSlab - 1) / kSlab;
-        // B slabs: rows p0 + 32 s .. of W (the pivot rows), words w0 ..
-        auto pivot_rows = [&](int64_t w0) {
-            return [=](uint32_t* dst, int sl) { q_load_kmajor_async<kQTileW>(dst, Wm, ldw, p0 + sl * kSlab, w0, tid); };
+        const uint32_t* src = pt == 0 ? E : S;  // tiles before this block's update
+        const bool last = pt == T - 1;
+        // B slabs: rows p0 + 32 s .. (the pivot rows), words w0 .., of `from`
+        auto pivot_rows = [&](const uint32_t* from, int64_t w0) {
+            return [=](uint32_t* dst, int sl) { q_load_kmajor_async<kQTileW>(dst, from, ldw, p0 + sl * kSlab, w0, tid); };
         };
         uint32_t c[8][4];
-        // 1. diagonal block: closure in registers; W and the resident A = Dg*
-        q_load_tile(c, Wm, ldw, p0, pw0, tx, ty);
+        // 1. diagonal block: closure in registers; S and the resident A = Dg*
+        q_load_tile(c, src, ldw, p0, pw0, tx, ty);
         q_close(c, Bst, Bst + 2 * kQTileW, kv, tx, ty);
-        q_store_tile(c, Wm, ldw, p0, pw0, tx, ty);
+        q_store_tile(c, S, ldw, p0, pw0, tx, ty);
+        if (last) q_store_tile_i32(c, G, n, p0, pw0, tx, ty, m);
         q_store_panel(c, Ap, tx, ty);
         __syncthreads();
-        // 2. row panel: W[P][J] = min(W[P][J], Dg* (x) W[P][J]), B the tile's own
-        //    rows (every thread has read them before the last slab's barrier,
+        // 2. row panel: S[P][J] = min(X[P][J], Dg* (x) X[P][J]), X = src: B the
+        //    tile's own rows before the update (in S from the second block on,
+        //    where every thread has read them before the last slab's barrier,
         //    so the stores after the loop are safe)
         for (int tj = 0; tj < T; ++tj) {
             if (tj == pt) continue;
             const int64_t w0 = (int64_t)tj * kQTileW;
-            q_load_tile(c, Wm, ldw, p0, w0, tx, ty);
-            q_mainloop(c, nslab, kv, Ap, Bst, pivot_rows(w0), tx, ty, one);
-            q_store_tile(c, Wm, ldw, p0, w0, tx, ty);
+            q_load_tile(c, src, ldw, p0, w0, tx, ty);
+            q_mainloop(c, nslab, kv, Ap, Bst, pivot_rows(src, w0), tx, ty, one);
+            q_store_tile(c, S, ldw, p0, w0, tx, ty);
+            if (last) q_store_tile_i32(c, G, n, p0, (int)w0, tx, ty, m);
             __syncthreads();  // the next tile's prologue refills the ring
         }
         // 3. tile row after tile row
         for (int ti = 0; ti < T; ++ti) {
             if (ti == pt) continue;
-            const int64_t r0 = (int64_t)ti * kTile;
-            const int rows = min(kTile, n - (int)r0);
-            // column panel W[I][P] = min(C, C (x) Dg*): A = C (pre-update), B = Dg* rows
-            q_load_tile(c, Wm, ldw, r0, pw0, tx, ty);
+            const int r0 = ti * kTile;
+            const int rows = min(kTile, n - r0);
+            // column panel min(C, C (x) Dg*): A = C (before the update), B = Dg* rows (S)
+            q_load_tile(c, src, ldw, r0, pw0, tx, ty);
             q_store_panel(c, Ap, tx, ty);
             __syncthreads();
-            q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(pw0), tx, ty, one);
+            q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(S, pw0), tx, ty, one);
             __syncthreads();  // every thread is done with A = C before it becomes C'
-            q_store_tile(c, Wm, ldw, r0, pw0, tx, ty);
+            if (last)
+                q_store_tile_i32(c, G, n, r0, pw0, tx, ty, m);
+            else
+                q_store_tile(c, S, ldw, r0, pw0, tx, ty);
             q_store_panel(c, Ap, tx, ty);
             __syncthreads();
-            // remainder W[I][J] = min(W[I][J], C' (x) W[P][J]), J != P
+            // remainder min(X[I][J], C' (x) S[P][J]), J != P
             for (int tj = 0; tj < T; ++tj) {
                 if (tj == pt) continue;
                 const int64_t w0 = (int64_t)tj * kQTileW;
-                q_load_tile(c, Wm, ldw, r0, w0, tx, ty);
-                q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(w0), tx, ty, one);
-                q_store_tile(c, Wm, ldw, r0, w0, tx, ty);
+                q_load_tile(c, src, ldw, r0, w0, tx, ty);
+                q_mainloop(c, nslab, rows, Ap, Bst, pivot_rows(S, w0), tx, ty, one);
+                if (last)
+                    q_store_tile_i32(c, G, n, r0, (int)w0, tx, ty, m);
+                else
+                    q_store_tile(c, S, ldw, r0, w0, tx, ty);
                 __syncthreads();  // the next tile's prologue refills the ring; the A panel is rewritten next
             }
         }
     }
+    return m;
 }
 
 }  // namespace fw

@@ -241,9 +241,10 @@ __device__ __forceinline__ void blocked_in_cta(int* __restrict__ Gm, int n, int6
 
 // Large graphs in the exact packed 16-bit form (fw_batch_p16.cuh): one CTA
 // per graph, persistent over items [start, start + count) (all with
-// 128 < n <= kQMaxN). A graph that does not qualify, or whose result the
-// proof cannot take, is left untouched and its item index appended to
-// `fallback` for the int32 kernel, which runs after this one.
+// 128 < n <= kQMaxN). A graph that does not qualify is left untouched; one
+// whose result the proof cannot take is restored to its input from the
+// encoded copy E. Either way its item index is appended to `fallback` for
+// the int32 kernel, which runs after this one.
 __global__ void __launch_bounds__(kThreads, 2)
     fw_batched_p16_kernel(int* __restrict__ packed, const BatchItem* __restrict__ items, int start, int count,
                           int* __restrict__ counters, int* __restrict__ fallback, uint32_t* __restrict__ ws,
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     extern __shared__ __align__(128) uint32_t qsm[];
     __shared__ int s_item;
     __shared__ QProof pf;
-    uint32_t* Wm = ws + (int64_t)blockIdx.x * ws_words;
+    uint32_t* E = ws + (int64_t)blockIdx.x * ws_words;
     const int tid = threadIdx.x;
     for (;;) {
         __syncthreads();  // the previous graph's readers of s_item and pf are done
@@ -268,20 +269,19 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int n = item.n;
         const int ld = (n + kTile - 1) / kTile * kTile;
         int* G = packed + item.offset;
-        q_encode(G, n, Wm, ld, &pf);
+        uint32_t* S = E + q_copy_words(ld);
+        q_encode(G, n, E, ld, &pf);
         __syncthreads();
-        bool take = pf.bad == 0;
+        bool take = pf.bad == 0;  // G untouched otherwise
         if (take) {
-            q_sweep(Wm, n, ld, qsm, one);
-            q_rmax(Wm, n, ld, &pf);
+            unsigned m = q_sweep(E, S, G, n, ld, qsm, one);  // writes the results into G
+            for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if ((tid & 31) == 0 && m) atomicMax(&pf.rmax, m);
             __syncthreads();
             take = pf.rmax + pf.wmax < kQCap;
+            if (!take) q_decode(E, G, n, ld);  // the proof failed: G back to the input
         }
-        if (take) {
-            q_decode(Wm, G, n, ld);
-        } else if (tid == 0) {
-            fallback[atomicAdd(&counters[kFallbackCount], 1)] = start + it;
-        }
+        if (!take && tid == 0) fallback[atomicAdd(&counters[kFallbackCount], 1)] = start + it;
     }
 }
 

@@ -33,13 +33,15 @@ constexpr int kSmemBytes = kStages * kStageInts * 4;     // 96 KB
 // (see relax2). Measured on GB300 with the TMA-fed remainder kernel, whole
 // multi-layer solves (kappa 8, n = 32768): the first k columns in form A,
 // 8 of 8 (DPX only) 1975 ms, 7 of 8 1918, 6 of 8 1797, 5 of 8 1806, 4 of 8
-// 1807, 3 of 8 1715, 2 of 8 1846, 1 of 8 2045 ms; then the six best sets of
-// three columns of a standalone-kernel sweep, each built into the library
-// and timed in one process: {1, 4, 6} 1683 ms, {0, 1, 2} 1717 ms, the others
-// 1759-1768 ms (same order at n = 16384 and 8192). Which columns take form A
-// changes how the compiler interleaves the two pipes.
+// 1807, 3 of 8 1715, 2 of 8 1846, 1 of 8 2045 ms. Then every set of two,
+// three and four columns (154 builds of the library timed in one process,
+// same matrix, bit-identical results): the fastest eight at n = 16384 re-timed
+// at n = 32768 gave {0, 2, 5, 6} 1662.5 ms, {1, 2, 4, 6} 1668.7, {1, 3, 4, 5}
+// 1673.7, {3, 4, 5, 6} 1674.6 ... {1, 4, 6} 1683.4 ms (at n = 16384 the best
+// pair of columns, {1, 4}, was 12 % slower than {0, 2, 5, 6}). Which columns
+// take form A changes how the compiler interleaves the two pipes.
 constexpr unsigned cols_below(int k) { return (1u << k) - 1u; }
-constexpr unsigned kColsA = (1u << 1) | (1u << 4) | (1u << 6);
+constexpr unsigned kColsA = (1u << 0) | (1u << 2) | (1u << 5) | (1u << 6);
 
 // Register micro-tile ownership inside a 128 x 128 tile (thread t, tx = t % 16,
 // ty = t / 16): rows ty*4 + {0..3} and 64 + ty*4 + {0..3}; columns
