@@ -242,26 +242,23 @@ __device__ __forceinline__ void p_load_transposed_dup(uint32_t* dst, const uint1
     }
 }
 
-// Number of the 8 word columns that fold a pivot pair with two packed DPX
-// add-mins; the others add with two 32-bit multiply-adds (exact as packed
-// adds: each half stays below 65535, so no carry crosses the halves) on the
-// FMA pipe and take one packed three-way DPX min. Measured on GB300 with the
-// TMA-fed remainder kernel (whole packed solve, n = 32768): 7 of 8 964 ms,
-// 6 of 8 942, 5 of 8 922, 4 of 8 884, 3 of 8 930, 2 of 8 978 ms.
-constexpr int kP16MixA = 4;
+// The word columns (bit w = column w of the thread's 8) that fold a pivot
+// pair with two packed DPX add-mins; the others add with two 32-bit
+// multiply-adds (exact as packed adds: each half stays below 65535, so no
+// carry crosses the halves) on the FMA pipe and take one packed three-way DPX
+// min. Measured on GB300 with the TMA-fed remainder kernel (whole packed
+// solve, n = 32768): the first k columns in form A, 7 of 8 964 ms, 6 of 8
+// 942, 5 of 8 922, 4 of 8 884, 3 of 8 930, 2 of 8 978 ms; of the sets of
+// four, the even columns 875 ms, columns 0-3 884, 2-5 894, {0,1,4,5} 895,
+// {0,3,4,7} 919, odd 933, 4-7 947 ms. Every set of two to six columns
+// (238 builds of the library timed in one process on the same matrix, all
+// results bit-identical) kept the even columns first: at n = 16384 113.1 ms
+// against 114.9 ms for the next ({1, 2, 3, 5}), and at n = 32768, for the
+// eight fastest, 868.9 ms against 884.4-894.7 ms. The choice changes how the
+// compiler schedules the two pipes.
+constexpr unsigned kP16ColsA = 0x55u;
 
-// Which word columns take the DPX form. With four of eight the even columns
-// do: the choice changes how the compiler schedules the two pipes (measured,
-// whole packed solve at n = 32768: even columns 875 ms, columns 0-3 884,
-// 2-5 894, {0,1,4,5} 895, {0,3,4,7} 919, odd 933, 4-7 947, rows 0-3 952,
-// checkerboard 989 ms; interleaved patterns of other counts: five columns
-// 899-927 ms, six 923-965, three 938 ms).
-template <int MIXW>
-__device__ constexpr bool p_dpx_column(int w) {
-    return MIXW == 4 ? (w & 1) == 0 : w < MIXW;
-}
-
-template <int MIXW>
+template <unsigned COLS>
 __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t* As, const uint32_t* Bs, int tx,
                                              int ty, int one) {
 #pragma unroll 1
@@ -287,7 +284,7 @@ __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t
         for (int r = 0; r < 8; ++r)
 #pragma unroll
             for (int w = 0; w < 8; ++w) {
-                if (p_dpx_column<MIXW>(w)) {
+                if ((COLS >> w) & 1u) {
                     c[r][w] = __viaddmin_u16x2(a1[r], b1[w], __viaddmin_u16x2(a0[r], b0[w], c[r][w]));
                 } else {
                     const uint32_t s0 = (uint32_t)add_on_fma((int)a0[r], (int)b0[w], one);
@@ -298,7 +295,7 @@ __device__ __forceinline__ void p_relax_slab(uint32_t (&c)[8][8], const uint32_t
     }
 }
 
-template <int MIXW = kP16MixA, class LA, class LB>
+template <unsigned COLS = kP16ColsA, class LA, class LB>
 __device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint32_t* smem, LA la, LB lb, int tx,
                                            int ty, int one) {
 #pragma unroll
@@ -320,7 +317,7 @@ __device__ __forceinline__ void p_mainloop(uint32_t (&c)[8][8], int nslab, uint3
         }
         cp_async_commit();
         const uint32_t* st = smem + (kb % kPStages) * kPStageWords;
-        p_relax_slab<MIXW>(c, st, st + kPSlabA, tx, ty, one);
+        p_relax_slab<COLS>(c, st, st + kPSlabA, tx, ty, one);
     }
 }
 
@@ -529,7 +526,7 @@ __device__ __forceinline__ void p_update_tile(uint16_t* __restrict__ D16, int64_
         }
         if (kb + kPStages - 1 < nslab) issue(kb + kPStages - 1);
         const uint32_t* stage = psm + stg * kPStageWords;
-        p_relax_slab<kP16MixA>(c, stage, stage + kPSlabA, tx, ty, one);
+        p_relax_slab<kP16ColsA>(c, stage, stage + kPSlabA, tx, ty, one);
     }
     p_store_tile(c, D16, ldw, r0, w0, tx, ty);
 }

@@ -227,7 +227,7 @@ int measure_relax_peak_packed(double* dpx_only, double* mixed, cudaStream_t s) {
     FW_CUDA_TRY(cudaMallocAsync(&out, (size_t)blocks * 256 * sizeof(unsigned), s));
     FW_CUDA_TRY(cudaMemsetAsync(in, 0, 768 * sizeof(unsigned), s));
     // MIXW = 8: every word column as two packed DPX add-mins; the others: the
-    // packed remainder's mix (kP16MixA) and its neighbours.
+    // packed remainder's count of DPX word columns (four) and its neighbours.
     double r8 = 0, r6 = 0, r5 = 0, r4 = 0, r3 = 0;
     int rc = time_peak_packed<8>(blocks, in, out, s, &r8);
     if (!rc) rc = time_peak_packed<6>(blocks, in, out, s, &r6);
