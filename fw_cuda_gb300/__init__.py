@@ -70,6 +70,7 @@ EXPORTED_SYMBOLS = (
     "fw_debug_inject",
     "fw_debug_bounded_wait",
     "fw_measure_int32_rates",
+    "fw_debug_flag_wait",
 )
 
 # Host-side fault injection kinds of fw_debug_inject (tests only).
@@ -175,6 +176,8 @@ def lib():
     L.fw_debug_bounded_wait.restype = c_int
     L.fw_measure_int32_rates.argtypes = [ctypes.POINTER(ctypes.c_double), c_int, vp]
     L.fw_measure_int32_rates.restype = c_int
+    L.fw_debug_flag_wait.argtypes = [i64, vp]
+    L.fw_debug_flag_wait.restype = c_int
     _lib = L
     return L
 
@@ -298,6 +301,12 @@ def debug_bounded_wait(spins: int, stream=None) -> int:
     """Test hook: a bounded wait on a copy that is never issued; returns the
     status (FW_ERR_TIMEOUT when the wait gave up, as it should)."""
     return int(lib().fw_debug_bounded_wait(spins, _stream(stream)))
+
+
+def debug_flag_wait(limit_us: int, stream=None) -> int:
+    """Test hook: the stripe sweep's bounded flag wait on a flag nothing sets;
+    returns the status (FW_ERR_TIMEOUT when the wait gave up, as it should)."""
+    return int(lib().fw_debug_flag_wait(limit_us, _stream(stream)))
 
 
 def version() -> str:

@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CUDA_SOURCES = ["fw_apsp_i32.cu", "fw_capi.cu", "fw_peak.cu", "fw_noalloc.cu", "fw_batched.cu", "fw_diff.cu", "fw_packed16.cu", "fw_graph_io.cu", "fw_ooc.cu", "fw_gen.cu"]
+CUDA_SOURCES = ["fw_apsp_i32.cu", "fw_capi.cu", "fw_peak.cu", "fw_noalloc.cu", "fw_batched.cu", "fw_diff.cu", "fw_packed16.cu", "fw_graph_io.cu", "fw_ooc.cu", "fw_gen.cu", "fw_stripe.cu"]
 HOST_LIB_SOURCES = ["algorithms.cpp"]  # compiled into libfw103.so
 TOOL_SOURCE = "runners.cpp"  # bench_runner / tests_runner (one binary, two names)
 TOOLS = ("bench_runner", "tests_runner")

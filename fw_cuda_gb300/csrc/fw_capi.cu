@@ -57,7 +57,8 @@ ProfState g_prof;
 const char* const kClassNames[KC_COUNT] = {"fw_diag",          "fw_panel",        "fw_remainder",
                                            "fw_pivot_step",    "fw_batched",      "fw_forward_f32",
                                            "fw_backward_f32",  "fw_p16_diag",     "fw_p16_panel",
-                                           "fw_p16_remainder", "fw_paths_i32",    "fw_ooc_update"};
+                                           "fw_p16_remainder", "fw_paths_i32",    "fw_ooc_update",
+                                           "fw_stripe"};
 
 cudaEvent_t prof_event() {
     if (g_prof.next == g_prof.pool.size()) {
@@ -245,7 +246,9 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     if (variant == FW_VARIANT_BASELINE) return kStatusBytes + pivot_workspace_bytes(n);
     const size_t blocked = blocked_workspace_bytes(n, 2);
     if (variant == FW_VARIANT_AUTO) return kStatusBytes + ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
-    return kStatusBytes + blocked;
+    // Small graphs run the stripe sweep when the workspace holds it.
+    const size_t stripe = stripe_workspace_bytes(n);
+    return kStatusBytes + (stripe > blocked ? stripe : blocked);
 }
 
 }  // extern "C"
@@ -261,7 +264,7 @@ size_t min_workspace_bytes(int64_t n, int kappa, int variant) {
 }
 
 int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
-                size_t workspace_bytes, fw_stream_t stream, bool may_allocate) {
+                size_t workspace_bytes, fw_stream_t stream, bool may_allocate, bool allow_stripe) {
     if (int rc = check_apsp_args(d_D, n, variant)) return rc;
     (void)tile;  // fixed geometry, as in the reference (src/fw_tiling_gpu.cu:254-257)
     const size_t need = min_workspace_bytes(n, kappa, variant);
@@ -280,6 +283,17 @@ int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void*
     unsigned int* faults = static_cast<unsigned int*>(status);
     if (int rc = status_begin(s, status)) return rc;
     int rc = FW_OK;
+    // The blocked variants take the stripe sweep (one cooperative launch) for
+    // n <= 2048 when the workspace has fw_workspace_bytes_i32() bytes; a
+    // smaller caller workspace keeps the 128-wide blocked sweep.
+    if (allow_stripe && (variant == FW_VARIANT_TILING || variant == FW_VARIANT_MULTI_LAYER) &&
+        stripe_workspace_bytes(n) > 0 && body_bytes >= stripe_workspace_bytes(n) &&
+        body_bytes >= blocked_workspace_bytes(n, 2)) {
+        bool ran = false;
+        rc = stripe_solve(d_D, n, body, s, faults, &ran);
+        if (rc) return rc;
+        if (ran) return status_end(s, status);
+    }
     if (variant == FW_VARIANT_BASELINE) {
         rc = pivot_solve(d_D, n, body, s, may_allocate);
     } else if (variant == FW_VARIANT_AUTO) {

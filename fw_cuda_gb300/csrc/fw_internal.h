@@ -64,6 +64,7 @@ enum KernelClass {
     KC_P16_REMAINDER,
     KC_PATHS_I32,
     KC_OOC_UPDATE,
+    KC_STRIPE,
     KC_COUNT
 };
 
@@ -128,6 +129,16 @@ int blocked_solve(int32_t* d_D, int64_t n, int blocks, void* ws, size_t ws_bytes
 // Smallest workspace fw_apsp_i32_ws accepts for these arguments.
 size_t min_workspace_bytes(int64_t n, int kappa, int variant);
 
+// Stripe sweep (fw_stripe.cu): the blocked sweep with 8-wide pivot blocks in
+// one cooperative launch, the matrix held in registers, for 1 <= n <= 2048.
+constexpr int64_t kStripeMaxN = 2048;
+// Workspace of the stripe sweep (0 when n is outside its range).
+size_t stripe_workspace_bytes(int64_t n);
+// Runs the stripe sweep when n is in range and the device can hold its
+// cooperative grid; *ran tells whether it did (if not, nothing was enqueued).
+// `faults`: the call's status word (flag waits that ran out add to it).
+int stripe_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s, unsigned int* faults, bool* ran);
+
 // Exact packed 16-bit fast path (fw_packed16.cu).
 size_t p16_workspace_bytes(int64_t n);
 // inject_copy_fault (tests): mark the packed status as if a tile copy had
@@ -138,9 +149,11 @@ size_t pivot_workspace_bytes(int64_t n);
 // may_allocate = false: plain launches only (no CUDA graph is captured,
 // which would allocate driver resources).
 int pivot_solve(int32_t* d_D, int64_t n, void* ws, cudaStream_t s, bool may_allocate = true);
-// fw_apsp_i32_ws; may_allocate = false for callers that must allocate nothing.
+// fw_apsp_i32_ws; may_allocate = false for callers that must allocate nothing;
+// allow_stripe = false keeps small graphs of the blocked variants on the
+// blocked sweep.
 int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void* d_workspace,
-                size_t workspace_bytes, fw_stream_t stream, bool may_allocate);
+                size_t workspace_bytes, fw_stream_t stream, bool may_allocate, bool allow_stripe = true);
 
 // Differentiable fp32 forward / backward (fw_diff.cu).
 size_t f32_workspace_bytes(int64_t n, int64_t batch);

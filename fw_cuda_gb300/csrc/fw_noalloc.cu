@@ -128,5 +128,5 @@ extern "C" int fw_apsp_i32_noalloc(int32_t* d_D, int64_t n, int tile, int kappa,
     // Passing exactly the minimum keeps the single-stream schedule (the
     // look-ahead would also create a side stream on first use), and the
     // per-pivot sweep launches directly instead of replaying a graph.
-    return fw::apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, need, stream, false);
+    return fw::apsp_i32_ws(d_D, n, tile, kappa, variant, scratch, need, stream, false, false);
 }

@@ -61,7 +61,12 @@ typedef enum fw_variant {
  * as in the reference; `kappa` is used by FW_VARIANT_MULTI_LAYER only, with
  * the reference's normalisation (<= 0 or > 16 becomes 4,
  * src/fw_multi_layer_tiling_gpu.cu:511-513). Uses a per-(device, stream)
- * workspace that the library allocates on first use and keeps. */
+ * workspace that the library allocates on first use and keeps.
+ * FW_VARIANT_TILING and FW_VARIANT_MULTI_LAYER with n <= 2048 run as one
+ * cooperative launch (the stripe sweep: 8-wide pivot blocks, the matrix held
+ * in registers across the SMs) when the device can hold its grid and the
+ * workspace has fw_workspace_bytes_i32() bytes; otherwise the 128-wide
+ * blocked sweep runs. Both give the same result. */
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
 
 /* After a FW_VARIANT_AUTO call on `stream`: synchronises the stream and sets
@@ -76,8 +81,13 @@ int fw_apsp_auto_report(fw_stream_t stream, int* used_packed);
 /* Bytes of device workspace fw_apsp_i32_ws needs for these arguments. */
 size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant);
 
-/* As fw_apsp_i32, with a caller-owned workspace of at least
- * fw_workspace_bytes_i32() bytes (256-byte aligned); allocates nothing. */
+/* As fw_apsp_i32, with a caller-owned workspace (256-byte aligned);
+ * allocates nothing. fw_workspace_bytes_i32() bytes select the fastest
+ * schedule (the stripe sweep for n <= 2048, the look-ahead or two-block pass
+ * of the blocked sweep above). The blocked variants also accept less, down to the 256-byte
+ * status block and one pair of 128-row panels (128 x (n rounded up to 128)
+ * ints each; two pairs for kappa > 4 at n >= 24576), which runs the 128-wide
+ * blocked sweep without its look-ahead. */
 int fw_apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant,
                    void* d_workspace, size_t workspace_bytes, fw_stream_t stream);
 
@@ -270,6 +280,14 @@ int fw_debug_inject(int kinds);
  * barrier is left balanced. Returns FW_ERR_TIMEOUT when the wait gave up (the
  * expected outcome), FW_OK if it did not. Synchronous. */
 int fw_debug_bounded_wait(int spins, fw_stream_t stream);
+
+/* Test hook: one thread runs the stripe sweep's bounded flag wait (the wait
+ * of the small-graph sweep for a pivot stripe another CTA publishes) on a
+ * flag that nothing sets, limited to `limit_us` microseconds (1 .. 1000000),
+ * then sets the flag and checks that the same wait sees it. Returns
+ * FW_ERR_TIMEOUT when the first wait gave up (the expected outcome), FW_OK if
+ * it did not. No counterpart in the reference. Synchronous. */
+int fw_debug_flag_wait(int64_t limit_us, fw_stream_t stream);
 
 /* Message of the last failure on this host thread ("" if none). */
 const char* fw_last_error_string(void);

@@ -98,6 +98,13 @@ def test_workspace_sizes(fw):
     assert fw.workspace_bytes_i32(32768, variant=2) == status + 2 * 256 * 32768 * 4
     assert fw.workspace_bytes_i32(32769, variant=2) == status + 2 * 256 * (32768 + 128) * 4
     assert fw.workspace_bytes_i32(32768, kappa=8, variant=1) == status + 2 * 256 * 32768 * 4
+    # n <= 2048 (blocked variants and AUTO): at least the stripe sweep's
+    # published pivot rows (8 * ceil(n / 8) rows of 128 * ceil(n / 128) ints)
+    # and one flag per stripe, each part rounded up to 256 bytes
+    assert fw.workspace_bytes_i32(1024, variant=1) == status + 128 * 8 * 1024 * 4 + 512
+    assert fw.workspace_bytes_i32(1000, variant=2) == status + 125 * 8 * 1024 * 4 + 512
+    assert fw.workspace_bytes_i32(2048, variant=2) == status + 256 * 8 * 2048 * 4 + 1024
+    assert fw.workspace_bytes_i32(2049, variant=2) == status + 2 * 256 * 2176 * 4
     # per-pivot: two row and two column snapshots
     assert fw.workspace_bytes_i32(1001, variant=0) == status + 4 * 1004 * 4
     assert fw.workspace_bytes_i32(0, variant=1) == 0
@@ -111,6 +118,9 @@ def test_fault_hooks_reject_bad_arguments(fw):
     for spins in (0, -1, (1 << 20) + 1):
         assert L.fw_debug_bounded_wait(spins, None) == fw.FW_ERR_INVALID_ARGUMENT
         assert b"spins" in L.fw_last_error_string()
+    for limit in (0, -5, 1000001):
+        assert L.fw_debug_flag_wait(limit, None) == fw.FW_ERR_INVALID_ARGUMENT
+        assert b"limit_us" in L.fw_last_error_string()
 
 
 def test_noalloc_rejects_before_device_work(fw):
