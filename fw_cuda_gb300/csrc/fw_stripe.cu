@@ -13,8 +13,8 @@
 //     the stripe's 8 rows of its 4 columns (one 16-byte vector per row);
 //   * stage z applies the 8 pivots of stripe z. Its owner closes the 8 x 8
 //     diagonal block Dg in one warp (shuffles), turns the stripe into
-//     R' = min(R, Dg* (x) R) (an in-place sweep over the 8 pivots, exact
-//     because Dg* is closed), writes R' to the workspace and releases flag z;
+//     R' = min(R, Dg* (x) R) (a min-plus product, because Dg* is closed),
+//     writes R' to the workspace and releases flag z;
 //   * every other stripe takes stage z as D = min(D, C (x) R'), where C is the
 //     stripe's own 8 columns of the pivots as they were BEFORE the stage.
 //     With Dg* closed, C' (x) R' = C (x) R' for C' = min(C, C (x) Dg*), and on
@@ -110,22 +110,29 @@ __device__ __forceinline__ int lane_of(const int4& v, int e) {
 // acc = min(acc, C (x) P) for one stripe: C the stripe's 8 values of the
 // stage's pivot columns per row (shared memory, row-major [8][8]), P the
 // stage's 8 published pivot rows at this thread's 4 columns (global, read
-// through L2 in two halves of 4 rows to keep registers low).
+// through L2). ONE_SHOT issues all 8 row loads at once (one L2 round trip on
+// the critical path); otherwise they come in two halves of 4 rows, which
+// keeps the registers of a two-stripe CTA low.
+template <bool ONE_SHOT>
 __device__ __forceinline__ void stripe_update(int (&acc)[kStripeRows][kStripeVec], const int* cs, const int* prow,
                                               int ldw, int one) {
+    constexpr int kRowsPerLoad = ONE_SHOT ? kStripeRows : kStripeRows / 2;
 #pragma unroll
-    for (int kh = 0; kh < 2; ++kh) {
-        int4 p[4];
+    for (int kh = 0; kh < kStripeRows; kh += kRowsPerLoad) {
+        int4 p[kRowsPerLoad];
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) p[kk] = ld_cg4(prow + (int64_t)(kh * 4 + kk) * ldw);
+        for (int kk = 0; kk < kRowsPerLoad; ++kk) p[kk] = ld_cg4(prow + (int64_t)(kh + kk) * ldw);
 #pragma unroll
         for (int r = 0; r < kStripeRows; ++r) {
-            const int4 c = *reinterpret_cast<const int4*>(cs + r * kStripeRows + kh * 4);
 #pragma unroll
-            for (int e = 0; e < kStripeVec; ++e) {
-                const bool fa = ((kStripeColsA >> e) & 1u) != 0;
-                int v = relax2(fa, acc[r][e], c.x, lane_of(p[0], e), c.y, lane_of(p[1], e), one);
-                acc[r][e] = relax2(fa, v, c.z, lane_of(p[2], e), c.w, lane_of(p[3], e), one);
+            for (int k4 = 0; k4 < kRowsPerLoad; k4 += 4) {
+                const int4 c = *reinterpret_cast<const int4*>(cs + r * kStripeRows + kh + k4);
+#pragma unroll
+                for (int e = 0; e < kStripeVec; ++e) {
+                    const bool fa = ((kStripeColsA >> e) & 1u) != 0;
+                    int v = relax2(fa, acc[r][e], c.x, lane_of(p[k4], e), c.y, lane_of(p[k4 + 1], e), one);
+                    acc[r][e] = relax2(fa, v, c.z, lane_of(p[k4 + 2], e), c.w, lane_of(p[k4 + 3], e), one);
+                }
             }
         }
     }
@@ -133,23 +140,28 @@ __device__ __forceinline__ void stripe_update(int (&acc)[kStripeRows][kStripeVec
 
 // Closes this CTA's stripe z (held in acc) and publishes it: Dg (the stripe's
 // pivot columns, held by threads 2z and 2z + 1) -> shared memory, closure by
-// warp 0, the in-place panel sweep R' = min(R, Dg* (x) R), R' -> the
-// workspace, then flag z. Called by every thread of the CTA.
+// the warp of those threads, the panel R' = min(R, Dg* (x) R) (PAIRS: from a copy of R, pivot
+// pairs on both pipes; otherwise an in-place sweep without the copy's
+// registers), R' -> the workspace, then flag z. Called by every thread of
+// the CTA.
+template <bool PAIRS>
 __device__ __forceinline__ void stripe_close_publish(int (&acc)[kStripeRows][kStripeVec], int z, int* dgt,
-                                                     int* piv, int ldw, unsigned* flags) {
+                                                     int* piv, int ldw, unsigned* flags, int one) {
     const int t = threadIdx.x;
-    // dgt[k][i] = Dg[i][k]: the block transposed, so that column k of Dg* is one row.
-    if ((t >> 1) == z) {
-        const int h = (t & 1) * kStripeVec;
+    // The warp that holds Dg (threads 2z and 2z + 1, one warp) closes it:
+    // dgt[k][i] = Dg[i][k] (the block transposed, so that column k of Dg* is
+    // one row), then per pivot lane (i, j), i < 4, relaxes Dg[i][j] (lo) and
+    // Dg[i + 4][j] (hi) from shuffled copies of row and column k.
+    if ((t >> 5) == ((2 * z) >> 5)) {
+        if ((t >> 1) == z) {
+            const int h = (t & 1) * kStripeVec;
 #pragma unroll
-        for (int e = 0; e < kStripeVec; ++e)
+            for (int e = 0; e < kStripeVec; ++e)
 #pragma unroll
-            for (int r = 0; r < kStripeRows; ++r) dgt[(h + e) * kStripeRows + r] = acc[r][e];
-    }
-    __syncthreads();
-    if (t < 32) {
-        // lane (i, j), i < 4: holds Dg[i][j] (lo) and Dg[i + 4][j] (hi)
-        const int i = t >> 3, j = t & 7;
+                for (int r = 0; r < kStripeRows; ++r) dgt[(h + e) * kStripeRows + r] = acc[r][e];
+        }
+        __syncwarp();
+        const int lane = t & 31, i = lane >> 3, j = lane & 7;
         int lo = dgt[j * kStripeRows + i], hi = dgt[j * kStripeRows + i + 4];
 #pragma unroll
         for (int k = 0; k < kStripeRows; ++k) {
@@ -165,22 +177,45 @@ __device__ __forceinline__ void stripe_close_publish(int (&acc)[kStripeRows][kSt
         dgt[j * kStripeRows + i + 4] = hi;
     }
     __syncthreads();
-    // R' = min(R, Dg* (x) R), in place over the pivots: pivot k relaxes every
-    // row through row k (exact, because Dg* is closed: every value it can
-    // produce is at least min(R, Dg* (x) R), and pivot k alone reaches
-    // Dg*[i][k] + R[k]).
-#pragma unroll
-    for (int k = 0; k < kStripeRows; ++k) {
-        const int4 g0 = *reinterpret_cast<const int4*>(dgt + k * kStripeRows);
-        const int4 g1 = *reinterpret_cast<const int4*>(dgt + k * kStripeRows + 4);
-        const int g[kStripeRows] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
-        int rk[kStripeVec];
-#pragma unroll
-        for (int e = 0; e < kStripeVec; ++e) rk[e] = acc[k][e];
+    if constexpr (PAIRS) {
+        // R' = min(R, Dg* (x) R) from a copy of R, two pivots per step over
+        // both integer pipes (relax2).
+        int rr[kStripeRows][kStripeVec];
 #pragma unroll
         for (int r = 0; r < kStripeRows; ++r)
 #pragma unroll
-            for (int e = 0; e < kStripeVec; ++e) acc[r][e] = __viaddmin_s32(g[r], rk[e], acc[r][e]);
+            for (int e = 0; e < kStripeVec; ++e) rr[r][e] = acc[r][e];
+#pragma unroll
+        for (int r = 0; r < kStripeRows; ++r) {
+            // row r of Dg*: dgt[k][r] for k = 0..7
+            int g[kStripeRows];
+#pragma unroll
+            for (int k = 0; k < kStripeRows; ++k) g[k] = dgt[k * kStripeRows + r];
+#pragma unroll
+            for (int k = 0; k < kStripeRows; k += 2)
+#pragma unroll
+                for (int e = 0; e < kStripeVec; ++e)
+                    acc[r][e] = relax2(((kStripeColsA >> e) & 1u) != 0, acc[r][e], g[k], rr[k][e], g[k + 1],
+                                       rr[k + 1][e], one);
+        }
+    } else {
+        // R' = min(R, Dg* (x) R), in place over the pivots: pivot k relaxes
+        // every row through row k (exact, because Dg* is closed: every value
+        // it can produce is at least min(R, Dg* (x) R), and pivot k alone
+        // reaches Dg*[i][k] + R[k]).
+#pragma unroll
+        for (int k = 0; k < kStripeRows; ++k) {
+            const int4 g0 = *reinterpret_cast<const int4*>(dgt + k * kStripeRows);
+            const int4 g1 = *reinterpret_cast<const int4*>(dgt + k * kStripeRows + 4);
+            const int g[kStripeRows] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+            int rk[kStripeVec];
+#pragma unroll
+            for (int e = 0; e < kStripeVec; ++e) rk[e] = acc[k][e];
+#pragma unroll
+            for (int r = 0; r < kStripeRows; ++r)
+#pragma unroll
+                for (int e = 0; e < kStripeVec; ++e) acc[r][e] = __viaddmin_s32(g[r], rk[e], acc[r][e]);
+        }
     }
     // The diagonal block itself is Dg*, as the closure left it (the same
     // values the sweep above produces there unless a cycle is negative; with
@@ -196,11 +231,11 @@ __device__ __forceinline__ void stripe_close_publish(int (&acc)[kStripeRows][kSt
 #pragma unroll
     for (int r = 0; r < kStripeRows; ++r)
         *reinterpret_cast<int4*>(dst + (int64_t)r * ldw) = make_int4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+    // The barrier orders every thread's row stores before thread 0's release
+    // store of the flag, and the release (gpu scope, cumulative) makes them
+    // visible to any CTA that acquires the flag.
     __syncthreads();
-    if (t == 0) {
-        __threadfence();
-        st_release_gpu(flags + z, 1u);
-    }
+    if (t == 0) st_release_gpu(flags + z, 1u);
 }
 
 template <int S, bool VEC>
@@ -230,7 +265,7 @@ __global__ void __launch_bounds__(StripeCfg<S>::kMaxThreads, 1)
             }
         }
     }
-    if (cta == 0) stripe_close_publish(acc[0], 0, dgt, piv, ldw, flags);
+    if (cta == 0) stripe_close_publish<S == 1>(acc[0], 0, dgt, piv, ldw, flags, one);
     for (int s = 0; s < ns; ++s) {
         const int buf = s & 1;
         const int own_s = (s % G == cta) ? s / G : -1;  // slot holding pivot stripe s
@@ -260,13 +295,13 @@ __global__ void __launch_bounds__(StripeCfg<S>::kMaxThreads, 1)
 #pragma unroll
         for (int q = 0; q < S; ++q) {
             if (q != own_n) continue;
-            stripe_update(acc[q], cs[buf][q], prow, ldw, one);
-            stripe_close_publish(acc[q], nx, dgt, piv, ldw, flags);
+            stripe_update<S == 1>(acc[q], cs[buf][q], prow, ldw, one);
+            stripe_close_publish<S == 1>(acc[q], nx, dgt, piv, ldw, flags, one);
         }
 #pragma unroll
         for (int q = 0; q < S; ++q) {
             if (q == own_s || q == own_n || cta + q * G >= ns) continue;
-            stripe_update(acc[q], cs[buf][q], prow, ldw, one);
+            stripe_update<S == 1>(acc[q], cs[buf][q], prow, ldw, one);
         }
     }
 #pragma unroll
