@@ -245,10 +245,11 @@ size_t fw_workspace_bytes_i32(int64_t n, int tile, int kappa, int variant) {
     if (n < 1) return 0;
     if (variant == FW_VARIANT_BASELINE) return kStatusBytes + pivot_workspace_bytes(n);
     const size_t blocked = blocked_workspace_bytes(n, 2);
-    if (variant == FW_VARIANT_AUTO) return kStatusBytes + ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n);
+    const size_t body =
+        variant == FW_VARIANT_AUTO ? ((blocked + 255) & ~size_t(255)) + p16_workspace_bytes(n) : blocked;
     // Small graphs run the stripe sweep when the workspace holds it.
     const size_t stripe = stripe_workspace_bytes(n);
-    return kStatusBytes + (stripe > blocked ? stripe : blocked);
+    return kStatusBytes + (stripe > body ? stripe : body);
 }
 
 }  // extern "C"
@@ -283,16 +284,26 @@ int apsp_i32_ws(int32_t* d_D, int64_t n, int tile, int kappa, int variant, void*
     unsigned int* faults = static_cast<unsigned int*>(status);
     if (int rc = status_begin(s, status)) return rc;
     int rc = FW_OK;
-    // The blocked variants take the stripe sweep (one cooperative launch) for
-    // n <= 2048 when the workspace has fw_workspace_bytes_i32() bytes; a
-    // smaller caller workspace keeps the 128-wide blocked sweep.
-    if (allow_stripe && (variant == FW_VARIANT_TILING || variant == FW_VARIANT_MULTI_LAYER) &&
-        stripe_workspace_bytes(n) > 0 && body_bytes >= stripe_workspace_bytes(n) &&
-        body_bytes >= blocked_workspace_bytes(n, 2)) {
+    // For n <= 2048 the blocked variants and AUTO take the stripe sweep (one
+    // cooperative launch; faster there than the packed path) when the
+    // workspace has fw_workspace_bytes_i32() bytes; a smaller caller workspace
+    // keeps the 128-wide blocked sweep, or the packed path for AUTO.
+    if (allow_stripe && variant != FW_VARIANT_BASELINE && stripe_workspace_bytes(n) > 0 &&
+        body_bytes >= stripe_workspace_bytes(n) && body_bytes >= blocked_workspace_bytes(n, 2)) {
         bool ran = false;
         rc = stripe_solve(d_D, n, body, s, faults, &ran);
         if (rc) return rc;
-        if (ran) return status_end(s, status);
+        if (ran) {
+            if (variant == FW_VARIANT_AUTO) {
+                // fw_apsp_auto_report reads a word of this call's status
+                // block that status_begin zeroed: the packed path did not run.
+                int dev = 0;
+                cudaGetDevice(&dev);
+                std::lock_guard<std::mutex> lk(g_ws_mutex);
+                g_auto_done[{dev, s}] = faults + 1;
+            }
+            return status_end(s, status);
+        }
     }
     if (variant == FW_VARIANT_BASELINE) {
         rc = pivot_solve(d_D, n, body, s, may_allocate);

@@ -339,9 +339,12 @@ StripeGeom stripe_geom(int64_t n) {
     return g;
 }
 
+// *launched = false (and FW_OK) when the device refuses the cooperative grid
+// (for instance when another process limits the SMs this one may use).
 template <int S, bool VEC>
 int stripe_launch(int32_t* D, int64_t n, const StripeGeom& g, int grid, int* piv, unsigned* flags, unsigned* faults,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool* launched) {
+    *launched = false;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)g.thr);
@@ -353,9 +356,15 @@ int stripe_launch(int32_t* D, int64_t n, const StripeGeom& g, int grid, int* piv
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     prof_begin(KC_STRIPE, s);
-    FW_CUDA_TRY(cudaLaunchKernelEx(&cfg, fw_stripe_kernel<S, VEC>, (int*)D, (int)n, g.ns, g.ldw, piv, flags, faults, 1,
-                                   kStripeWaitNs));
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fw_stripe_kernel<S, VEC>, (int*)D, (int)n, g.ns, g.ldw, piv, flags,
+                                             faults, 1, kStripeWaitNs);
+    if (e == cudaErrorCooperativeLaunchTooLarge) {
+        cudaGetLastError();
+        return FW_OK;
+    }
+    if (e != cudaSuccess) return cuda_error(e, "fw_stripe_kernel (cooperative launch)");
     prof_end(KC_STRIPE, s, (double)n * (double)n * (double)n);
+    *launched = true;
     return FW_OK;
 }
 
@@ -381,16 +390,14 @@ int stripe_solve_impl(int32_t* D, int64_t n, void* ws, cudaStream_t s, unsigned*
     if (int rc = resident_ctas<1, VEC>(g.thr, &cap1)) return rc;
     if (g.ns <= cap1 && g.thr <= StripeCfg<1>::kMaxThreads) {
         FW_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)g.ns * sizeof(unsigned), s));
-        *ran = true;
-        return stripe_launch<1, VEC>(D, n, g, g.ns, piv, flags, faults, s);
+        return stripe_launch<1, VEC>(D, n, g, g.ns, piv, flags, faults, s, ran);
     }
     int cap2 = 0;
     if (int rc = resident_ctas<2, VEC>(g.thr, &cap2)) return rc;
     if (g.thr <= StripeCfg<2>::kMaxThreads && cap2 > 0 && g.ns <= kStripeMaxSlots * cap2) {
         const int grid = g.ns < cap2 ? g.ns : cap2;
         FW_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)g.ns * sizeof(unsigned), s));
-        *ran = true;
-        return stripe_launch<2, VEC>(D, n, g, grid, piv, flags, faults, s);
+        return stripe_launch<2, VEC>(D, n, g, grid, piv, flags, faults, s, ran);
     }
     return FW_OK;  // does not fit this device: the caller runs the blocked sweep
 }

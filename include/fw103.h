@@ -48,7 +48,8 @@ typedef enum fw_variant {
     FW_VARIANT_BASELINE = 0,    /* "baseline_gpu": one relaxation sweep per pivot */
     FW_VARIANT_TILING = 1,      /* "tiling_gpu": blocked sweep, 128-wide pivot blocks */
     FW_VARIANT_MULTI_LAYER = 2, /* "multi_layer_tiling_gpu": kappa pivot layers per pass */
-    FW_VARIANT_AUTO = 3         /* exact packed 16-bit sweep when provably identical, else MULTI_LAYER */
+    FW_VARIANT_AUTO = 3         /* n <= 2048: the int32 stripe sweep; larger: exact packed 16-bit
+                                   sweep when provably identical, else MULTI_LAYER */
 } fw_variant;
 
 /* ---------------------------------------------------------------- plain APSP */
@@ -62,17 +63,19 @@ typedef enum fw_variant {
  * the reference's normalisation (<= 0 or > 16 becomes 4,
  * src/fw_multi_layer_tiling_gpu.cu:511-513). Uses a per-(device, stream)
  * workspace that the library allocates on first use and keeps.
- * FW_VARIANT_TILING and FW_VARIANT_MULTI_LAYER with n <= 2048 run as one
- * cooperative launch (the stripe sweep: 8-wide pivot blocks, the matrix held
- * in registers across the SMs) when the device can hold its grid and the
- * workspace has fw_workspace_bytes_i32() bytes; otherwise the 128-wide
- * blocked sweep runs. Both give the same result. */
+ * With n <= 2048, FW_VARIANT_TILING, FW_VARIANT_MULTI_LAYER and
+ * FW_VARIANT_AUTO run as one cooperative launch (the stripe sweep: 8-wide
+ * pivot blocks, the matrix held in registers across the SMs) when the device
+ * can hold its grid and the workspace has fw_workspace_bytes_i32() bytes;
+ * otherwise the 128-wide blocked sweep (or, for AUTO, the packed path) runs.
+ * All give the same result. */
 int fw_apsp_i32(int32_t* d_D, int64_t n, int tile, int kappa, int variant, fw_stream_t stream);
 
 /* After a FW_VARIANT_AUTO call on `stream`: synchronises the stream and sets
  * *used_packed to 1 if the exact packed 16-bit sweep produced the result, 0 if
- * the int32 sweep ran (input outside [0, 32767) u {INF}, or distances too
- * close to the 16-bit cap to prove the packed result exact). The answer lives
+ * an int32 sweep ran (the stripe sweep for n <= 2048, or input outside
+ * [0, 32767) u {INF}, or distances too close to the 16-bit cap to prove the
+ * packed result exact). The answer lives
  * in the call's workspace: ask before freeing a caller workspace
  * (fw_apsp_i32_ws); a library workspace that a later, larger call on the
  * stream replaced makes this return FW_ERR_INVALID_ARGUMENT. */

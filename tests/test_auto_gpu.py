@@ -1,7 +1,10 @@
-"""FW_VARIANT_AUTO: the exact packed 16-bit sweep is used only when its result
-is provably the int32 result; every case here must equal the oracle bit for
-bit, and the path taken must be the one the eligibility rule predicts."""
+"""FW_VARIANT_AUTO: for n <= 2048 the int32 stripe sweep (faster there than
+the packed path); above that the exact packed 16-bit sweep, used only when its
+result is provably the int32 result. Every case here must equal the oracle
+bit for bit, and the path taken must be the one the rule predicts."""
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import pytest
@@ -12,6 +15,12 @@ INF = 1_000_000_000
 AUTO = 3
 
 
+def reference(oracle, W):
+    out = np.ascontiguousarray(W, dtype=np.int32).copy()
+    oracle.fw_i32_pivots(out, 0, out.shape[0], threads=os.cpu_count() or 1)
+    return out
+
+
 def run_auto(fw, torch, W, kappa=4):
     n = W.shape[0]
     d = torch.from_numpy(np.ascontiguousarray(W, dtype=np.int32)).cuda()
@@ -20,20 +29,31 @@ def run_auto(fw, torch, W, kappa=4):
     return d.cpu().numpy(), used
 
 
-@pytest.mark.parametrize("n", [1, 2, 255, 256, 257, 511, 513, 1000, 1536])
+@pytest.mark.parametrize("n", [2049, 2100, 2303, 2304, 2305, 2560, 3000])
 def test_small_weights_take_the_packed_path(fw, cuda, oracle, n):
     W = oracle.generate_graph(n, 0.5, 77 + n, 1, 100)
     out, used = run_auto(fw, cuda, W)
-    assert np.array_equal(out, oracle.fw_i32(W))
+    assert np.array_equal(out, reference(oracle, W))
     assert used
 
 
+@pytest.mark.parametrize("n", [1, 2, 255, 513, 1000, 2048])
+def test_up_to_2048_the_stripe_sweep_runs(fw, cuda, oracle, n):
+    W = oracle.generate_graph(n, 0.5, 77 + n, 1, 100)
+    fw.profile_begin()
+    out, used = run_auto(fw, cuda, W)
+    ran = fw.profile_end()
+    assert np.array_equal(out, reference(oracle, W))
+    assert not used
+    assert "fw_stripe" in ran and "fw_p16_remainder" not in ran and "fw_p16_diag" not in ran
+
+
 def test_unreachable_pairs_decode_to_inf(fw, cuda, oracle):
-    n = 600
+    n = 2200
     W = oracle.generate_graph(n, 0.02, 5, 0, 100)  # sparse: many unreachable pairs, zero weights too
-    W[:300, 300:] = INF  # no edge from the first half to the second
+    W[: n // 2, n // 2:] = INF  # no edge from the first half to the second
     np.fill_diagonal(W, 0)
-    ref = oracle.fw_i32(W)
+    ref = reference(oracle, W)
     assert np.count_nonzero(ref == INF) > 0
     out, used = run_auto(fw, cuda, W)
     assert np.array_equal(out, ref)
@@ -41,17 +61,18 @@ def test_unreachable_pairs_decode_to_inf(fw, cuda, oracle):
 
 
 def test_reference_weight_range(fw, cuda, oracle):
-    W = oracle.generate_graph(700, 0.9, 42, 0, 25000)
+    W = oracle.generate_graph(2200, 0.9, 42, 0, 25000)
     out, _ = run_auto(fw, cuda, W)
-    assert np.array_equal(out, oracle.fw_i32(W))
+    assert np.array_equal(out, reference(oracle, W))
 
 
 @pytest.mark.parametrize("case", ["negative", "too_large", "long_paths"])
 def test_ineligible_inputs_fall_back_exactly(fw, cuda, oracle, case):
-    n = 300
+    n = 2100
     W = oracle.generate_graph(n, 0.3, 9, 1, 100)
     if case == "negative":
-        W[3, 7] = -5
+        # every way back from 7 to 3 weighs at least 2, so no cycle is negative
+        W[3, 7] = -1
         W[7, 3] = 10
     elif case == "too_large":
         W[1, 2] = 40000  # finite but above the 16-bit range
@@ -61,17 +82,17 @@ def test_ineligible_inputs_fall_back_exactly(fw, cuda, oracle, case):
         for i in range(n - 1):
             W[i, i + 1] = 20000
     out, used = run_auto(fw, cuda, W)
-    assert np.array_equal(out, oracle.fw_i32(W))
+    assert np.array_equal(out, reference(oracle, W))
     assert not used
 
 
 def test_kappa_8_fallback_and_repeat(fw, cuda, oracle):
-    W = oracle.generate_graph(900, 0.3, 3, 1, 100)
+    W = oracle.generate_graph(2200, 0.3, 3, 1, 100)
     W[0, 1] = -1
-    ref = oracle.fw_i32(W)
+    ref = reference(oracle, W)
     for _ in range(2):
         out, used = run_auto(fw, cuda, W, kappa=8)
         assert np.array_equal(out, ref) and not used
-    W2 = oracle.generate_graph(900, 0.3, 4, 1, 100)
+    W2 = oracle.generate_graph(2200, 0.3, 4, 1, 100)
     out, used = run_auto(fw, cuda, W2, kappa=8)
-    assert np.array_equal(out, oracle.fw_i32(W2)) and used
+    assert np.array_equal(out, reference(oracle, W2)) and used

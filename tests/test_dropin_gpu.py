@@ -165,9 +165,10 @@ def test_cpp_shim_exits_on_injected_miss(fw, cuda, name):
 
 
 def test_injected_packed_miss_falls_back_to_int32(fw, cuda, oracle):
-    n = 1000
+    n = 2200  # above 2048, where AUTO takes the packed path
     W = fw.generate_graph(n, 0.5, 21, 1, 100)
-    ref = oracle.fw_i32(W)
+    ref = W.copy()
+    oracle.fw_i32_pivots(ref, 0, n, threads=os.cpu_count() or 1)
     d = cuda.from_numpy(W).cuda()
     fw.apsp_i32(d, n, 32, 8, fw.VARIANT_AUTO, None)
     assert fw.auto_used_packed(None)

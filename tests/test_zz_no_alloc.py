@@ -72,7 +72,7 @@ def test_noalloc_allocates_no_device_memory(fw, cuda, n, variant):
 
 def test_noalloc_auto_runs_int32_and_drops_the_auto_report(fw, cuda):
     f = _noalloc(fw)
-    n = 500
+    n = 2100  # above 2048, where the allocating entry point's AUTO takes the packed path
     W = fw.generate_graph(n, 0.5, 78, 1, 100)
     s = cuda.cuda.Stream()
     d = cuda.from_numpy(W).cuda()
