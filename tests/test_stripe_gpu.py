@@ -55,7 +55,7 @@ def test_matches_oracle(fw, cuda, oracle, n):
         assert np.array_equal(out, ref), (n, variant, kappa, int(np.count_nonzero(out != ref)))
 
 
-@pytest.mark.parametrize("n", [8, 129, 1000, 1217, 2048])
+@pytest.mark.parametrize("n", [1, 2, 8, 31, 127, 128, 129, 255, 257, 300, 513, 777, 1000, 1023, 1217, 2047, 2048])
 def test_equals_blocked_sweep(fw, cuda, oracle, n):
     """The blocked minimum of workspace keeps the 128-wide blocked sweep; both
     schedules give the same matrix."""
