@@ -13,7 +13,8 @@ What is written:
   fwBaselineCPU actually returns.
 * ``reference_cases.json`` — for each randomized case of the reference's test
   suites (src/tests.cpp:156-159, src/tests_gpu.cu:172-180) and for the
-  BASELINE workloads with integer weights in [1, 100]: SHA-256 of the input
+  benchmark workloads with integer weights in [1, 100] (n = 1024 and
+  n = 8192, density 0.9, seed 42): SHA-256 of the input
   matrix and of fwBaselineCPU's output (int32, row-major, little-endian).
   Inputs of the randomized cases come from the reference's own generator
   (src/graph_generator.cpp:48-80); the [1, 100] inputs, which that generator
@@ -78,7 +79,7 @@ KNOWN = [
 RANDOM_CASES = [(128, 0.9, 42), (256, 0.9, 123), (512, 0.9, 456), (1024, 0.9, 789),
                 (128, 0.1, 101), (256, 0.1, 202), (512, 0.1, 303), (1024, 0.1, 404)]
 
-# BASELINE workloads with integer weights in [1, 100].
+# Benchmark workloads with integer weights in [1, 100]: n = 1024 and 8192, density 0.9, seed 42.
 WEIGHTED_CASES = [("C1", 1024, 0.9, 42)]
 LARGE_CASES = [("C2", 8192, 0.9, 42)]
 

@@ -4,7 +4,8 @@ Cases follow the reference's own suites (src/tests_gpu.cu:76-185): the six
 known-answer matrices, the eight randomized graphs (n = 128..1024, density
 0.9 and 0.1) compared by hash with the reference's fwBaselineCPU output, plus
 ragged sizes around every tile boundary, negative weights without negative
-cycles, negative cycles, and the BASELINE workloads.
+cycles, negative cycles, and the benchmark workloads at n = 1024 and n = 8192
+(density 0.9, weights 1..100, seed 42).
 """
 from __future__ import annotations
 
