@@ -80,8 +80,8 @@ RANDOM_CASES = [(128, 0.9, 42), (256, 0.9, 123), (512, 0.9, 456), (1024, 0.9, 78
                 (128, 0.1, 101), (256, 0.1, 202), (512, 0.1, 303), (1024, 0.1, 404)]
 
 # Benchmark workloads with integer weights in [1, 100]: n = 1024 and 8192, density 0.9, seed 42.
-WEIGHTED_CASES = [("C1", 1024, 0.9, 42)]
-LARGE_CASES = [("C2", 8192, 0.9, 42)]
+WEIGHTED_CASES = [("w1-100_n1024_d0.9_s42", 1024, 0.9, 42)]
+LARGE_CASES = [("w1-100_n8192_d0.9_s42", 8192, 0.9, 42)]
 
 
 def main() -> None:

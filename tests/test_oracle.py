@@ -41,7 +41,7 @@ def test_small_full_matrices(oracle):
 
 
 @pytest.mark.parametrize("case_id", ["ref_gen_n128_d0.9_s42", "ref_gen_n256_d0.1_s202",
-                                     "ref_gen_n512_d0.9_s456", "ref_gen_n1024_d0.1_s404", "C1"])
+                                     "ref_gen_n512_d0.9_s456", "ref_gen_n1024_d0.1_s404", "w1-100_n1024_d0.9_s42"])
 def test_reference_hashes(oracle, case_id):
     cases = {c["id"]: c for c in load_json("reference_cases.json")["cases"]}
     c = cases[case_id]

@@ -118,22 +118,25 @@ def test_negative_cycle_detected_and_deterministic(fw, cuda, oracle, n):
         assert np.array_equal(out1, out2)  # no races: the same input gives the same output
 
 
-def test_config_c1(fw, cuda):
+def test_n1024_weights_1_100(fw, cuda):
     """n=1024, density 0.9, weights [1, 100], seed 42 vs the reference baseline_cpu."""
-    c = {c["id"]: c for c in load_json("reference_cases.json")["cases"]}["C1"]
+    c = {c["id"]: c for c in load_json("reference_cases.json")["cases"]}["w1-100_n1024_d0.9_s42"]
     a = fw.generate_graph(1024, 0.9, 42, 1, 100)
     assert sha(a) == c["input_sha256"]
     for v in VARIANTS.values():
         assert sha(solve(fw, cuda, a, v, kappa=4)) == c["output_sha256"], v
 
 
-def test_config_c2_kappa_sweep(fw, cuda, oracle):
+N8192 = "w1-100_n8192_d0.9_s42"
+
+
+def test_n8192_kappa_sweep(fw, cuda, oracle):
     """n=8192, density 0.9, weights [1, 100], seed 42; kappa in {1,2,4,6,8}."""
     cases = {c["id"]: c for c in load_json("reference_cases.json")["cases"]}
     a = fw.generate_graph(8192, 0.9, 42, 1, 100)
-    want = cases["C2"]["output_sha256"] if "C2" in cases else None
+    want = cases[N8192]["output_sha256"] if N8192 in cases else None
     if want is not None:
-        assert sha(a) == cases["C2"]["input_sha256"]
+        assert sha(a) == cases[N8192]["input_sha256"]
     outs = set()
     for kappa in (1, 2, 4, 6, 8):
         outs.add(sha(solve(fw, cuda, a, 2, kappa=kappa)))
